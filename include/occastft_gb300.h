@@ -1,0 +1,132 @@
+/*
+ * occastft_gb300 — C ABI of the GB300 (sm_103a) STFT runner.
+ *
+ * This library is the drop-in for OCCAstft's CUDA runner: the calls below
+ * replace, one for one, what the reference's runner contract exposes
+ * (StandAlone/cross_gpgpu/GLOBAL/RunnerInterface.hpp) and what its CUDA
+ * vendor implementation does (StandAlone/cross_gpgpu/CUDA/src/CudaImpl.cpp,
+ * StandAlone/cross_gpgpu/CUDA/src/functionImpl.cpp).  Signatures use plain
+ * pointers and sizes only; `stream` arguments are cudaStream_t handles passed
+ * as void* (NULL = the legacy default stream).
+ *
+ * Option strings follow the reference grammar (RunnerCommon.cpp:166-253):
+ *   --hanning_window --hamming_window --blackman_window --nuttall_window
+ *   --blackman_nuttall_window --blackman_harris_window --flattop_window
+ *   --gaussian_window=<sigma><<sigma   --remove_dc   --half_complex_return
+ * with the reference's precedence (first window in that order wins) and its
+ * sigma parsing.  Two additive flags select a layout the reference lacks:
+ *   --layout=dense   N/2+1 bins per frame (power: qt*(N/2+1) floats,
+ *                    half-complex: qt*(N/2+1) interleaved complex)
+ *   --serial_power   power = sqrt(2)*|Re X|, the value the reference's
+ *                    Serial/OpenMP runners return (default: |X|, the value
+ *                    of the reference's toPower kernel)
+ *
+ * All entry points are thread-safe.  Status codes: OCS_OK or one of OCS_E*;
+ * ocs_last_error() then holds the message (for pipeline failures it is the
+ * reference's own status string, e.g. "Operation not supported" or
+ * "--gaussian_window").
+ */
+#ifndef OCCASTFT_GB300_H
+#define OCCASTFT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OCS_OK 0
+#define OCS_EINVAL 1    /* unsupported size/overlap/option ("Operation not supported") */
+#define OCS_EPIPELINE 2 /* the option string fails the reference's parsing ("--gaussian_window") */
+#define OCS_ENOMEM 3    /* device or pinned-host allocation failed / admission refused */
+#define OCS_ECUDA 4     /* a CUDA call failed */
+#define OCS_ESPACE 5    /* the output buffer is smaller than the layout needs */
+#define OCS_ETIMEDOUT 6 /* a bounded device wait expired */
+
+/* Frame geometry of one request (all values as the reference computes them). */
+typedef struct ocs_geometry {
+    uint32_t qt;          /* frame count, toQuot() */
+    uint32_t hop;         /* OMove */
+    uint32_t ofull;       /* OFullSize = qt * N */
+    uint32_t ohalf;       /* OHalfSize = OFullSize / 2 */
+    uint32_t n_window;    /* N = 1 << windowSizeEXP */
+    uint32_t reserved;
+    uint64_t out_floats;  /* floats the selected layout writes */
+    uint64_t frames;      /* frames the device computes (compat half-complex needs only ceil(qt/2)) */
+} ocs_geometry;
+
+/* Runner::InitEnv + Runner::BuildKernel (CudaImpl.cpp:285-407): select the
+ * device, size launch grids.  Calling it is optional (the first request
+ * initialises the current device). */
+int ocs_init(int device);
+
+/* Runner::UnInit: release every cached plan, buffer and stream. */
+void ocs_shutdown(void);
+
+/* Message of the last failing call on this thread ("" when none). */
+const char* ocs_last_error(void);
+
+const char* ocs_version(void);
+
+/* Sizes of a request: toQuot (RunnerInterface.hpp:26-35) and the sizing block
+ * of ActivateSTFT (CudaImpl.cpp:416-421), plus the output length the options
+ * select. */
+int ocs_geometry_get(uint64_t n, int window_size_exp, float overlap_ratio, const char* options,
+                     ocs_geometry* out);
+
+/* Runner::ActivateSTFT (RunnerInterface.hpp:124-128; CUDA version
+ * CudaImpl.cpp:410-510): host signal in, host result out, synchronous.
+ * out must hold geometry.out_floats floats; *out_len receives that count.
+ * Host buffers from ocs_host_alloc give the fastest copies. */
+int ocs_activate(const float* in, uint64_t n, int window_size_exp, float overlap_ratio, const char* options,
+                 float* out, uint64_t out_cap, uint64_t* out_len);
+
+/* The device half of ActivateSTFT: runnerFunction::Default_Pipeline
+ * (RunnerCommon.cpp:184-316) on device-resident buffers, fused into one
+ * kernel launch on `stream`, asynchronous. */
+int ocs_activate_device(const float* d_in, uint64_t n, int window_size_exp, float overlap_ratio,
+                        const char* options, float* d_out, uint64_t out_cap, void* stream);
+
+/* The window coefficients the runner applies (host computation, no device
+ * needed): the reference's formulas (OKL/kernel.okl:33-127) evaluated with
+ * the same float/double roundings as its Serial runner, so they match that
+ * runner bit for bit on the same host.  kind as in ocs_stage_window;
+ * out receives window_size floats. */
+int ocs_window_table(int kind, uint32_t window_size, float sigma, float* out);
+
+/* Pinned host memory for inputs/outputs of ocs_activate. */
+int ocs_host_alloc(void** ptr, size_t bytes);
+int ocs_host_free(void* ptr);
+
+/* ---- per-stage hooks: runnerFunction::* (RunnerInterface.hpp:38-76) on
+ * device buffers laid out as the reference's [qt][N] planes. ---- */
+
+/* runnerFunction::Overlap (CUDA/src/functionImpl.cpp:15-55) */
+int ocs_stage_overlap(const float* d_origin, uint32_t ofull, uint32_t full_size, uint32_t window_size_exp,
+                      uint32_t hop, float* d_real, void* stream);
+
+/* runnerFunction::Hanning .. FlatTop, Gaussian (functionImpl.cpp:58-270);
+ * kind: 1 Hanning, 2 Hamming, 3 Blackman, 4 Nuttall, 5 Blackman-Nuttall,
+ * 6 Blackman-Harris, 7 FlatTop, 8 Gaussian(sigma) */
+int ocs_stage_window(int kind, float* d_data, uint32_t ofull, uint32_t window_size, float sigma, void* stream);
+
+/* runnerFunction::RemoveDC (functionImpl.cpp:276-305) */
+int ocs_stage_remove_dc(float* d_data, uint32_t qt, uint32_t ofull, uint32_t window_size, void* stream);
+
+/* runnerFunction::EXP6..EXP11 and EXPC (functionImpl.cpp:346-609): FFT of
+ * each frame of the real plane (imaginary input ignored, as the reference's
+ * first stage does), full N-bin spectra written back into d_real/d_imag. */
+int ocs_stage_fft(float* d_real, float* d_imag, uint32_t ohalf, uint32_t window_size_exp, void* stream);
+
+/* runnerFunction::HalfComplex (functionImpl.cpp:612-647) */
+int ocs_stage_half_complex(float* d_out, const float* d_real, const float* d_imag, uint32_t ohalf,
+                           uint32_t window_size_exp, void* stream);
+
+/* runnerFunction::ToPower (functionImpl.cpp:650-683) */
+int ocs_stage_to_power(float* d_out, const float* d_real, const float* d_imag, uint32_t ofull, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OCCASTFT_GB300_H */

@@ -1,0 +1,547 @@
+// C ABI of the GB300 STFT runner (include/occastft_gb300.h).
+//
+// Replaces the CUDA vendor runner of OCCAstft
+// (StandAlone/cross_gpgpu/CUDA/src/CudaImpl.cpp, functionImpl.cpp): where the
+// reference allocates, copies, runs 7+ kernels, copies back and frees on
+// every request, this runner keeps per-exponent plans (twiddle tables built
+// once in FP64 on the device, window tables built once on the host) and
+// request slots (streams + grow-only device buffers) resident, runs the
+// whole pipeline as one fused kernel, and overlaps host->device copies,
+// compute and device->host copies across frame chunks.
+#include "../../include/occastft_gb300.h"
+#include "ocs_host.h"
+#include "ocs_kernels.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg)
+{
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where)
+{
+    return fail(OCS_ECUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define OCS_CUDA(call)                                          \
+    do {                                                        \
+        cudaError_t _e = (call);                                \
+        if (_e != cudaSuccess) return cuda_fail(_e, #call);     \
+    } while (0)
+
+struct Slot {
+    cudaStream_t s_h2d = nullptr, s_comp = nullptr, s_d2h = nullptr;
+    std::vector<cudaEvent_t> ev_in, ev_comp;
+    float* d_in = nullptr;
+    size_t in_cap = 0;   // floats
+    float* d_out = nullptr;
+    size_t out_cap = 0;  // floats
+};
+
+constexpr int kMaxChunks = 16;
+
+struct Context {
+    std::mutex mu;
+    bool ready = false;
+    int device = -1;
+    int sms = 0;
+    cudaStream_t s_setup = nullptr;
+    std::map<int, float2*> twiddles;                             // exp -> table
+    std::map<std::tuple<int, int, uint32_t>, float*> windows;    // (kind, exp, sigma bits) -> table
+    std::map<std::pair<int, int>, int> occupancy;                // (exp, vec2) -> CTAs per SM
+    std::vector<Slot*> free_slots;
+    std::vector<Slot*> all_slots;
+};
+
+Context& ctx()
+{
+    static Context* c = new Context();  // never destroyed: outlives static teardown order
+    return *c;
+}
+
+int init_locked(Context& c, int device)
+{
+    if (c.ready) {
+        if (device >= 0 && device != c.device) return fail(OCS_EINVAL, "ocs_init: already initialised on another device");
+        OCS_CUDA(cudaSetDevice(c.device));
+        return OCS_OK;
+    }
+    if (device < 0) OCS_CUDA(cudaGetDevice(&device));
+    OCS_CUDA(cudaSetDevice(device));
+    cudaDeviceProp p;
+    OCS_CUDA(cudaGetDeviceProperties(&p, device));
+    if (p.major < 10) return fail(OCS_EINVAL, "this runner is built for sm_103a (Blackwell Ultra)");
+    c.device = device;
+    c.sms = p.multiProcessorCount;
+    OCS_CUDA(cudaStreamCreateWithFlags(&c.s_setup, cudaStreamNonBlocking));
+    c.ready = true;
+    return OCS_OK;
+}
+
+int ensure_init()
+{
+    Context& c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    return init_locked(c, c.ready ? c.device : -1);
+}
+
+int get_twiddles(int exp, const float2** out)
+{
+    Context& c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    auto it = c.twiddles.find(exp);
+    if (it != c.twiddles.end()) {
+        *out = it->second;
+        return OCS_OK;
+    }
+    float2* d = nullptr;
+    const int n = ocs::fused_twiddle_count(exp);
+    OCS_CUDA(cudaMalloc(&d, sizeof(float2) * n));
+    OCS_CUDA(ocs::build_twiddles(d, exp, c.s_setup));
+    OCS_CUDA(cudaStreamSynchronize(c.s_setup));
+    c.twiddles[exp] = d;
+    *out = d;
+    return OCS_OK;
+}
+
+int get_window(int kind, int exp, float sigma, const float** out)
+{
+    *out = nullptr;
+    if (kind == ocs::WIN_NONE) return OCS_OK;
+    Context& c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    uint32_t sbits = 0;
+    if (kind == ocs::WIN_GAUSSIAN) std::memcpy(&sbits, &sigma, 4);
+    const auto key = std::make_tuple(kind, exp, sbits);
+    auto it = c.windows.find(key);
+    if (it != c.windows.end()) {
+        *out = it->second;
+        return OCS_OK;
+    }
+    const std::vector<float> w = ocs::window_table(kind, 1 << exp, sigma);
+    float* d = nullptr;
+    OCS_CUDA(cudaMalloc(&d, sizeof(float) * w.size()));
+    OCS_CUDA(cudaMemcpyAsync(d, w.data(), sizeof(float) * w.size(), cudaMemcpyHostToDevice, c.s_setup));
+    OCS_CUDA(cudaStreamSynchronize(c.s_setup));
+    c.windows[key] = d;
+    *out = d;
+    return OCS_OK;
+}
+
+int grid_size(int exp, bool vec2, uint64_t frames)
+{
+    Context& c = ctx();
+    int occ;
+    {
+        std::lock_guard<std::mutex> lk(c.mu);
+        auto key = std::make_pair(exp, (int)vec2);
+        auto it = c.occupancy.find(key);
+        if (it == c.occupancy.end()) {
+            occ = std::max(1, ocs::fused_occupancy(exp, vec2));
+            c.occupancy[key] = occ;
+        } else {
+            occ = it->second;
+        }
+    }
+    const uint64_t fpc = (uint64_t)ocs::fused_frames_per_cta(exp);
+    const uint64_t need = (frames + fpc - 1) / fpc;
+    const uint64_t full = (uint64_t)c.sms * occ;
+    return (int)std::max<uint64_t>(1, std::min(need, full));
+}
+
+struct Request {
+    ocs::Options opt;
+    ocs::Geometry geo;
+    int exp = 0;
+};
+
+int prepare(uint64_t n, int exp, float ov, const char* options, Request& r)
+{
+    std::string st = ocs::parse_options(options, r.opt);
+    if (st != "OK") return fail(OCS_EPIPELINE, st);
+    st = ocs::make_geometry(n, exp, ov, r.opt, r.geo);
+    if (st != "OK") return fail(OCS_EINVAL, st);
+    r.exp = exp;
+    return OCS_OK;
+}
+
+// Launch the fused kernel for frames [f0, f1) of a request.
+int launch_frames(const Request& r, const float* d_sig, uint64_t n, float* d_out, uint64_t f0, uint64_t f1,
+                  cudaStream_t st)
+{
+    const float2* tw = nullptr;
+    const float* win = nullptr;
+    int rc = get_twiddles(r.exp, &tw);
+    if (rc) return rc;
+    rc = get_window(r.opt.window, r.exp, r.opt.sigma, &win);
+    if (rc) return rc;
+    const uint64_t N = r.geo.n_window;
+    const uint64_t hop = r.geo.hop;
+    const uint64_t start = f0 * hop;
+    ocs::FusedArgs a{};
+    a.x = d_sig + std::min<uint64_t>(start, n);
+    a.n = start < n ? n - start : 0;
+    a.hop = hop;
+    a.frames = f1 - f0;
+    a.win = win;
+    a.tw = tw;
+    a.mode = r.opt.half_complex ? ocs::OCS_MODE_HALF_COMPLEX : ocs::OCS_MODE_POWER;
+    a.dense = r.opt.dense;
+    a.serial_power = r.opt.serial_power;
+    a.remove_dc = r.opt.remove_dc;
+    if (r.opt.dense) {
+        const uint64_t row = (N / 2 + 1) * (r.opt.half_complex ? 2 : 1);
+        a.out = d_out + f0 * row;
+        a.ohalf = 0;
+    } else if (r.opt.half_complex) {
+        a.out = d_out + 2 * f0 * N;
+        a.ohalf = (uint64_t)r.geo.ohalf - f0 * N;
+    } else {
+        a.out = d_out + f0 * N;
+        a.ohalf = 0;
+    }
+    if (a.frames == 0) return OCS_OK;
+    if (start >= n) {
+        // frames entirely past the signal end still produce (zero) output
+        a.x = d_sig;
+        a.n = 0;
+    }
+    const bool vec2 = (hop % 2 == 0) && ((reinterpret_cast<uintptr_t>(a.x) & 7u) == 0);
+    const int grid = grid_size(r.exp, vec2, a.frames);
+    OCS_CUDA(ocs::launch_fused(r.exp, vec2, a, grid, st));
+    return OCS_OK;
+}
+
+// output floats of frames [f0, f1)
+void out_range(const Request& r, uint64_t f0, uint64_t f1, uint64_t* off, uint64_t* cnt)
+{
+    const uint64_t N = r.geo.n_window;
+    if (r.opt.dense) {
+        const uint64_t row = (N / 2 + 1) * (r.opt.half_complex ? 2 : 1);
+        *off = f0 * row;
+        *cnt = (f1 - f0) * row;
+    } else if (r.opt.half_complex) {
+        const uint64_t lim = 2ull * r.geo.ohalf;
+        const uint64_t a = std::min(2 * f0 * N, lim), b = std::min(2 * f1 * N, lim);
+        *off = a;
+        *cnt = b - a;
+    } else {
+        *off = f0 * N;
+        *cnt = (f1 - f0) * N;
+    }
+}
+
+Slot* acquire_slot(int* rc)
+{
+    Context& c = ctx();
+    {
+        std::lock_guard<std::mutex> lk(c.mu);
+        if (!c.free_slots.empty()) {
+            Slot* s = c.free_slots.back();
+            c.free_slots.pop_back();
+            return s;
+        }
+    }
+    Slot* s = new Slot();
+    cudaError_t e = cudaSuccess;
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->s_h2d, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->s_comp, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->s_d2h, cudaStreamNonBlocking);
+    for (int i = 0; i < kMaxChunks && e == cudaSuccess; ++i) {
+        cudaEvent_t a, b;
+        e = cudaEventCreateWithFlags(&a, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b, cudaEventDisableTiming);
+        if (e == cudaSuccess) {
+            s->ev_in.push_back(a);
+            s->ev_comp.push_back(b);
+        }
+    }
+    if (e != cudaSuccess) {
+        *rc = cuda_fail(e, "slot creation");
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lk(c.mu);
+    c.all_slots.push_back(s);
+    return s;
+}
+
+void release_slot(Slot* s)
+{
+    Context& c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    c.free_slots.push_back(s);
+}
+
+int grow(float** p, size_t* cap, size_t need)
+{
+    if (*cap >= need) return OCS_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    cudaError_t e = cudaMalloc(p, need * sizeof(float));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return fail(OCS_ENOMEM, std::string("device allocation failed: ") + cudaGetErrorString(e));
+    }
+    *cap = need;
+    return OCS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ocs_init(int device)
+{
+    Context& c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    return init_locked(c, device);
+}
+
+void ocs_shutdown(void)
+{
+    Context& c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    if (!c.ready) return;
+    cudaSetDevice(c.device);
+    cudaDeviceSynchronize();
+    for (auto& kv : c.twiddles) cudaFree(kv.second);
+    for (auto& kv : c.windows) cudaFree(kv.second);
+    c.twiddles.clear();
+    c.windows.clear();
+    for (Slot* s : c.all_slots) {
+        cudaStreamDestroy(s->s_h2d);
+        cudaStreamDestroy(s->s_comp);
+        cudaStreamDestroy(s->s_d2h);
+        for (auto e : s->ev_in) cudaEventDestroy(e);
+        for (auto e : s->ev_comp) cudaEventDestroy(e);
+        if (s->d_in) cudaFree(s->d_in);
+        if (s->d_out) cudaFree(s->d_out);
+        delete s;
+    }
+    c.all_slots.clear();
+    c.free_slots.clear();
+    c.occupancy.clear();
+    if (c.s_setup) cudaStreamDestroy(c.s_setup);
+    c.s_setup = nullptr;
+    c.ready = false;
+}
+
+const char* ocs_last_error(void) { return g_err.c_str(); }
+
+const char* ocs_version(void) { return "occastft_gb300 0.1 (sm_103a)"; }
+
+int ocs_geometry_get(uint64_t n, int exp, float ov, const char* options, ocs_geometry* out)
+{
+    Request r;
+    int rc = prepare(n, exp, ov, options, r);
+    if (rc) return rc;
+    std::memset(out, 0, sizeof(*out));
+    out->qt = r.geo.qt;
+    out->hop = r.geo.hop;
+    out->ofull = r.geo.ofull;
+    out->ohalf = r.geo.ohalf;
+    out->n_window = r.geo.n_window;
+    out->out_floats = r.geo.out_floats;
+    out->frames = r.geo.frames;
+    return OCS_OK;
+}
+
+int ocs_activate_device(const float* d_in, uint64_t n, int exp, float ov, const char* options, float* d_out,
+                        uint64_t out_cap, void* stream)
+{
+    Request r;
+    int rc = prepare(n, exp, ov, options, r);
+    if (rc) return rc;
+    if (out_cap < r.geo.out_floats) return fail(OCS_ESPACE, "output buffer too small");
+    if (!d_in || !d_out) return fail(OCS_EINVAL, "null buffer");
+    rc = ensure_init();
+    if (rc) return rc;
+    return launch_frames(r, d_in, n, d_out, 0, r.geo.frames, (cudaStream_t)stream);
+}
+
+int ocs_activate(const float* in, uint64_t n, int exp, float ov, const char* options, float* out, uint64_t out_cap,
+                 uint64_t* out_len)
+{
+    Request r;
+    int rc = prepare(n, exp, ov, options, r);
+    if (rc) return rc;
+    if (out_cap < r.geo.out_floats) return fail(OCS_ESPACE, "output buffer too small");
+    if (!in || !out) return fail(OCS_EINVAL, "null buffer");
+    rc = ensure_init();
+    if (rc) return rc;
+    Slot* s = acquire_slot(&rc);
+    if (!s) return rc;
+    const uint64_t N = r.geo.n_window, hop = r.geo.hop, F = r.geo.frames;
+    // samples the computed frames read
+    const uint64_t need_in = std::min<uint64_t>(n, (F - 1) * hop + N);
+    rc = grow(&s->d_in, &s->in_cap, std::max<uint64_t>(need_in, 1));
+    if (!rc) rc = grow(&s->d_out, &s->out_cap, std::max<uint64_t>(r.geo.out_floats, 1));
+    if (rc) {
+        release_slot(s);
+        return rc;
+    }
+    // chunking: ~8 MB of input per chunk, at most kMaxChunks
+    const uint64_t target = std::max<uint64_t>(1, (8ull << 20) / 4 / std::max<uint64_t>(hop, 1));
+    uint64_t chunks = std::min<uint64_t>(kMaxChunks, std::max<uint64_t>(1, (F + target - 1) / target));
+    const uint64_t per = (F + chunks - 1) / chunks;
+    chunks = (F + per - 1) / per;
+    uint64_t copied = 0;
+    cudaError_t e = cudaSuccess;
+    for (uint64_t ci = 0; ci < chunks && e == cudaSuccess; ++ci) {
+        const uint64_t f0 = ci * per, f1 = std::min(F, f0 + per);
+        const uint64_t hi = std::min<uint64_t>(need_in, (f1 - 1) * hop + N);
+        if (hi > copied) {
+            e = cudaMemcpyAsync(s->d_in + copied, in + copied, (hi - copied) * sizeof(float), cudaMemcpyHostToDevice,
+                                s->s_h2d);
+            copied = hi;
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(s->ev_in[ci], s->s_h2d);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s->s_comp, s->ev_in[ci], 0);
+        if (e != cudaSuccess) break;
+        rc = launch_frames(r, s->d_in, need_in, s->d_out, f0, f1, s->s_comp);
+        if (rc) break;
+        e = cudaEventRecord(s->ev_comp[ci], s->s_comp);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s->s_d2h, s->ev_comp[ci], 0);
+        uint64_t off, cnt;
+        out_range(r, f0, f1, &off, &cnt);
+        if (e == cudaSuccess && cnt)
+            e = cudaMemcpyAsync(out + off, s->d_out + off, cnt * sizeof(float), cudaMemcpyDeviceToHost, s->s_d2h);
+    }
+    cudaError_t e2 = cudaStreamSynchronize(s->s_d2h);
+    cudaError_t e3 = cudaStreamSynchronize(s->s_comp);
+    release_slot(s);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "ocs_activate");
+    if (e2 != cudaSuccess) return cuda_fail(e2, "ocs_activate sync");
+    if (e3 != cudaSuccess) return cuda_fail(e3, "ocs_activate sync");
+    if (out_len) *out_len = r.geo.out_floats;
+    return OCS_OK;
+}
+
+int ocs_window_table(int kind, uint32_t window_size, float sigma, float* out)
+{
+    if (kind < 1 || kind > 8 || !out || window_size < 2 || (window_size & (window_size - 1)))
+        return fail(OCS_EINVAL, "window table: bad arguments");
+    const std::vector<float> w = ocs::window_table(kind, (int)window_size, sigma);
+    std::memcpy(out, w.data(), sizeof(float) * w.size());
+    return OCS_OK;
+}
+
+int ocs_host_alloc(void** ptr, size_t bytes)
+{
+    cudaError_t e = cudaHostAlloc(ptr, bytes, cudaHostAllocPortable);
+    if (e != cudaSuccess) {
+        *ptr = nullptr;
+        return fail(OCS_ENOMEM, std::string("pinned allocation failed: ") + cudaGetErrorString(e));
+    }
+    return OCS_OK;
+}
+
+int ocs_host_free(void* ptr)
+{
+    OCS_CUDA(cudaFreeHost(ptr));
+    return OCS_OK;
+}
+
+// ---------------------------------------------------------------- stage hooks
+int ocs_stage_overlap(const float* d_origin, uint32_t ofull, uint32_t full_size, uint32_t exp, uint32_t hop,
+                      float* d_real, void* stream)
+{
+    if (exp < 6 || exp > 30 || !d_origin || !d_real || full_size == 0) return fail(OCS_EINVAL, "Overlap: bad arguments");
+    int rc = ensure_init();
+    if (rc) return rc;
+    OCS_CUDA(ocs::launch_overlap(d_origin, ofull, full_size, exp, hop, d_real, (cudaStream_t)stream));
+    return OCS_OK;
+}
+
+int ocs_stage_window(int kind, float* d_data, uint32_t ofull, uint32_t window_size, float sigma, void* stream)
+{
+    if (kind < 1 || kind > 8 || !d_data || window_size < 64 || (window_size & (window_size - 1)))
+        return fail(OCS_EINVAL, "window: bad arguments");
+    int exp = 0;
+    while ((1u << exp) < window_size) ++exp;
+    if (exp > 15) return fail(OCS_EINVAL, "window: size above 2^15");
+    int rc = ensure_init();
+    if (rc) return rc;
+    const float* w = nullptr;
+    rc = get_window(kind, exp, sigma, &w);
+    if (rc) return rc;
+    OCS_CUDA(ocs::launch_apply_window(d_data, w, ofull, window_size, (cudaStream_t)stream));
+    return OCS_OK;
+}
+
+int ocs_stage_remove_dc(float* d_data, uint32_t qt, uint32_t ofull, uint32_t window_size, void* stream)
+{
+    (void)qt;
+    if (!d_data || window_size < 64 || (window_size & (window_size - 1))) return fail(OCS_EINVAL, "RemoveDC: bad arguments");
+    int rc = ensure_init();
+    if (rc) return rc;
+    OCS_CUDA(ocs::launch_remove_dc(d_data, ofull, window_size, (cudaStream_t)stream));
+    return OCS_OK;
+}
+
+int ocs_stage_fft(float* d_real, float* d_imag, uint32_t ohalf, uint32_t exp, void* stream)
+{
+    if (exp < 6) return fail(OCS_EINVAL, "Operation not supported");
+    if (exp > 15) return fail(OCS_EINVAL, "Operation not supported: window sizes above 2^15");
+    if (!d_real || !d_imag) return fail(OCS_EINVAL, "EXP: null buffer");
+    int rc = ensure_init();
+    if (rc) return rc;
+    const float2* tw = nullptr;
+    rc = get_twiddles((int)exp, &tw);
+    if (rc) return rc;
+    const uint64_t N = 1ull << exp;
+    ocs::FusedArgs a{};
+    a.x = d_real;
+    a.n = 2ull * ohalf;
+    a.hop = N;
+    a.frames = 2ull * ohalf / N;
+    a.win = nullptr;
+    a.tw = tw;
+    a.out = d_real;
+    a.out_im = d_imag;
+    a.mode = ocs::OCS_MODE_PLANES;
+    if (a.frames == 0) return OCS_OK;
+    const bool vec2 = (reinterpret_cast<uintptr_t>(d_real) & 7u) == 0;
+    OCS_CUDA(ocs::launch_fused((int)exp, vec2, a, grid_size((int)exp, vec2, a.frames), (cudaStream_t)stream));
+    return OCS_OK;
+}
+
+int ocs_stage_half_complex(float* d_out, const float* d_real, const float* d_imag, uint32_t ohalf, uint32_t exp,
+                           void* stream)
+{
+    (void)exp;
+    if (!d_out || !d_real || !d_imag) return fail(OCS_EINVAL, "HalfComplex: null buffer");
+    int rc = ensure_init();
+    if (rc) return rc;
+    OCS_CUDA(ocs::launch_half_complex(d_out, d_real, d_imag, ohalf, (cudaStream_t)stream));
+    return OCS_OK;
+}
+
+int ocs_stage_to_power(float* d_out, const float* d_real, const float* d_imag, uint32_t ofull, void* stream)
+{
+    if (!d_out || !d_real || !d_imag) return fail(OCS_EINVAL, "ToPower: null buffer");
+    int rc = ensure_init();
+    if (rc) return rc;
+    OCS_CUDA(ocs::launch_to_power(d_out, d_real, d_imag, ofull, (cudaStream_t)stream));
+    return OCS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,166 @@
+"""Parity of the CUDA path (called through the C ABI) with the oracle and the
+reference's golden vectors.
+
+Bars (the benchmark spec): frame count, offsets, window choice and output layout
+bit-exact; FP32 spectra within REL_L2 = 1e-5 relative L2 of the FP64 oracle
+and of the reference's Serial output (where that output is not the known
+odd-exponent defect)."""
+import hashlib
+
+import numpy as np
+import pytest
+
+from tests.conftest import signal
+
+REL_L2 = 1e-5
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def runner(ocs_lib):
+    return ocs_lib.Runner(0)
+
+
+def _p4(exp):
+    return exp >= 13 and exp % 2 == 1
+
+
+def test_golden_cases(ocs_lib, orc, golden, runner):
+    manifest, arrays = golden
+    n_checked = 0
+    for c in manifest["cases"]:
+        x = signal(c["seed"], c["n"])
+        if c["status"] != "OK":
+            out = runner.ActivateSTFT(x, c["exp"], c["overlap"], c["options"])
+            assert out is None and runner.last_status == c["status"], c["name"]
+            continue
+        # the Serial runner's power is sqrt(2)|Re X|: ask for that layout
+        opts = c["options"] + ("" if "--half_complex_return" in c["options"] else " --serial_power")
+        got = runner.ActivateSTFT(x, c["exp"], c["overlap"], opts)
+        assert got is not None, (c["name"], runner.last_status)
+        assert got.size == c["ofull"], c["name"]
+        f64 = orc.fp64_stft(x, c["exp"], c["overlap"], opts)
+        assert orc.rel_l2(got, f64) <= REL_L2, c["name"]
+        fixed = orc.serial_pipeline(x, c["exp"], c["overlap"], c["options"], fix_p4=True)
+        assert orc.rel_l2(got, fixed) <= REL_L2, c["name"]
+        if not _p4(c["exp"]):
+            assert orc.rel_l2(got, arrays[c["name"]]) <= REL_L2, c["name"]
+        n_checked += 1
+    assert n_checked >= 30
+
+
+@pytest.mark.parametrize("exp", list(range(6, 16)))
+@pytest.mark.parametrize("opts", [
+    "--hamming_window",
+    "--blackman_window --half_complex_return",
+    "--hanning_window --remove_dc --layout=dense",
+    "--hanning_window --remove_dc --half_complex_return --layout=dense",
+])
+def test_each_window_size_vs_fp64(ocs_lib, orc, exp, opts):
+    N = 1 << exp
+    x = signal(exp * 7 + len(opts), 9 * N + 123)
+    for ov in (0.5, 0.75):
+        got = ocs_lib.activate(x, exp, ov, opts)
+        ref = orc.fp64_stft(x, exp, ov, opts)
+        assert got.size == ref.size
+        assert orc.rel_l2(got, ref) <= REL_L2, (exp, ov, opts)
+
+
+def test_c0_config(ocs_lib, orc, golden):
+    """C0: 2^20 samples, N=1024 Hann, overlap 0.5, DC removal, power, 2049x1024."""
+    manifest, arrays = golden
+    c = manifest["c0"]
+    x = signal(c["seed"], c["n"])
+    got = ocs_lib.activate(x, c["exp"], c["overlap"], c["options"] + " --serial_power")
+    assert got.size == 2049 * 1024
+    N = 1024
+    for i, f in enumerate(c["frames"]):
+        assert orc.rel_l2(got[f * N:(f + 1) * N], arrays["c0_frames"][i]) <= REL_L2, f
+    ser = orc.serial_pipeline(x, c["exp"], c["overlap"], c["options"], nthreads=8)
+    assert orc.rel_l2(got, ser) <= REL_L2
+    mag = ocs_lib.activate(x, c["exp"], c["overlap"], c["options"])
+    f64 = orc.fp64_stft(x, c["exp"], c["overlap"], c["options"])
+    assert orc.rel_l2(mag, f64) <= REL_L2
+    assert orc.max_db_error(mag, f64) < 0.01
+
+
+@pytest.mark.parametrize("n,exp,ov,opts", [
+    (1, 6, 0.5, "--hanning_window --remove_dc"),
+    (63, 6, 0.5, "--hamming_window"),
+    (100, 10, 0.5, "--hanning_window --half_complex_return"),
+    (3001, 8, 0.5 + 1 / 256, "--blackman_window --remove_dc"),   # odd hop: scalar loads
+    (2000, 7, -0.5, "--hanning_window"),                          # hop > N: gaps
+    (70001, 9, 0.3, "--flattop_window --remove_dc --half_complex_return"),
+    (50000, 11, 0.0, "--gaussian_window=x0.4<<sigma"),
+    (40000, 12, 0.875, "--nuttall_window"),
+    (5000, 8, 0.5, ""),
+])
+def test_ragged_and_edge_shapes(ocs_lib, orc, n, exp, ov, opts):
+    x = signal(n + exp, n)
+    got = ocs_lib.activate(x, exp, ov, opts)
+    ref = orc.fp64_stft(x, exp, ov, opts)
+    assert got.size == ref.size == ocs_lib.geometry(n, exp, ov, opts).out_floats
+    assert orc.rel_l2(got, ref) <= REL_L2
+
+
+def test_compat_half_complex_tail_untouched(ocs_lib):
+    """Compat half-complex fills exactly OFullSize floats; the layout is the
+    flat first OHalfSize bins (odd frame counts end mid-frame)."""
+    x = signal(4, 5 * 512 + 10)
+    g = ocs_lib.geometry(x.size, 9, 0.5, "--half_complex_return")
+    assert g.qt % 2 == 1
+    out = np.full(g.out_floats + 64, np.nan, dtype=np.float32)
+    got = ocs_lib.activate(x, 9, 0.5, "--half_complex_return", out=out)
+    assert got.size == g.ofull and not np.isnan(got).any()
+    assert np.isnan(out[g.ofull:]).all()
+
+
+def test_device_path_matches_host_path(ocs_lib):
+    import torch
+
+    x = signal(11, 300000)
+    for exp, opts in ((10, "--hanning_window --remove_dc"), (12, "--blackman_window --half_complex_return"),
+                      (7, "--hamming_window --layout=dense")):
+        g = ocs_lib.geometry(x.size, exp, 0.5, opts)
+        d_in = torch.from_numpy(x).cuda()
+        d_out = torch.full((g.out_floats + 16,), float("nan"), device="cuda")
+        ocs_lib.activate_device(d_in, x.size, exp, 0.5, opts, d_out, g.out_floats)
+        torch.cuda.synchronize()
+        host = ocs_lib.activate(x, exp, 0.5, opts)
+        dev = d_out.cpu().numpy()
+        assert np.array_equal(dev[: g.out_floats].view(np.uint32), host.view(np.uint32))
+        assert np.isnan(dev[g.out_floats:]).all()
+
+
+def test_unaligned_device_input(ocs_lib, orc):
+    import torch
+
+    x = signal(12, 20001)
+    buf = torch.zeros(x.size + 1, device="cuda")
+    buf[1:] = torch.from_numpy(x).cuda()
+    view = buf[1:]
+    opts = "--hanning_window --remove_dc"
+    g = ocs_lib.geometry(x.size, 9, 0.5, opts)
+    d_out = torch.empty(g.out_floats, device="cuda")
+    ocs_lib.activate_device(view, x.size, 9, 0.5, opts, d_out, g.out_floats)
+    torch.cuda.synchronize()
+    assert orc.rel_l2(d_out.cpu().numpy(), orc.fp64_stft(x, 9, 0.5, opts)) <= REL_L2
+
+
+def test_deterministic(ocs_lib):
+    x = signal(13, 1 << 18)
+    a = ocs_lib.activate(x, 11, 0.5, "--hanning_window --remove_dc")
+    b = ocs_lib.activate(x, 11, 0.5, "--hanning_window --remove_dc")
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_output_capacity_error(ocs_lib):
+    import torch
+
+    x = signal(14, 10000)
+    g = ocs_lib.geometry(x.size, 8, 0.5, "")
+    d_in = torch.from_numpy(x).cuda()
+    d_out = torch.empty(g.out_floats, device="cuda")
+    with pytest.raises(ocs_lib.OcsError) as ei:
+        ocs_lib.activate_device(d_in, x.size, 8, 0.5, "", d_out, g.out_floats - 1)
+    assert ei.value.code == ocs_lib.OCS_ESPACE

@@ -1,0 +1,38 @@
+"""Live pin: the oracle restatement against the reference's own Serial and
+OpenMP code compiled from source (oracle/build_ref.sh).  Skipped where the
+reference checkout was not available to build oracle/_ref/."""
+import numpy as np
+import pytest
+
+from tests.conftest import signal
+
+ref_missing = pytest.mark.skipif(
+    not __import__("oracle.orc", fromlist=["RefLib"]).RefLib.available(), reason="oracle/_ref not built")
+
+
+@ref_missing
+@pytest.mark.parametrize("exp", list(range(6, 16)))
+def test_oracle_matches_reference_serial(orc, exp):
+    R = orc.RefLib("libref_serial.so")
+    rng = np.random.default_rng(exp)
+    opts = ["--hanning_window --remove_dc", "--blackman_window --half_complex_return", "--hamming_window",
+            "--flattop_window --remove_dc --half_complex_return", "--gaussian_window=x3.5<<sigma", ""]
+    for ov in (0.0, 0.5, 0.75, 0.3):
+        for op in opts:
+            n = int(rng.integers(1 << exp, (1 << exp) * 6))
+            x = signal(int(rng.integers(1 << 30)), n)
+            ref, st = R.activate(x, exp, ov, op)
+            assert st == "OK"
+            mine = orc.serial_pipeline(x, exp, ov, op)
+            assert np.array_equal(ref.view(np.uint32), mine.view(np.uint32)), (exp, ov, op)
+
+
+@ref_missing
+def test_openmp_equals_serial(orc):
+    S = orc.RefLib("libref_serial.so")
+    O = orc.RefLib("libref_openmp.so")
+    x = signal(3, 50000)
+    for exp in (6, 10, 12, 13):
+        a, _ = S.activate(x, exp, 0.5, "--hanning_window --remove_dc")
+        b, _ = O.activate(x, exp, 0.5, "--hanning_window --remove_dc")
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
