@@ -273,7 +273,9 @@ def run_ours(args):
     n = N_SAMPLES
     x = make_signal_torch(n)
     geo = ocs.geometry(n, HEAD_EXP, HEAD_OV, HEAD_OPTS)
-    d_out = torch.empty(geo.out_floats, device="cuda")
+    # room for the largest output of the sweep (window 2^15, overlap 0.5)
+    cap = max(geo.out_floats, ocs.geometry(n, 15, 0.5, "").out_floats)
+    d_out = torch.empty(cap, device="cuda")
     peak, peak_kind = load_peaks()
 
     def barrier():
@@ -332,7 +334,7 @@ def run_ours(args):
 
     # end to end through the public host API (pinned host buffers)
     e2e = None
-    if rank == 0 or ws > 1:
+    if not args.no_e2e:
         import ctypes
 
         L = ocs.lib()
@@ -452,9 +454,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--n", type=int, default=N_SAMPLES, help="signal samples (profiling runs use fewer)")
+    ap.add_argument("--exp", type=int, default=HEAD_EXP)
+    ap.add_argument("--options", default=HEAD_OPTS)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    globals().update(N_SAMPLES=args.n, HEAD_EXP=args.exp, HEAD_OPTS=args.options)
     if args.impl == "reference":
         run_reference_arm(args)
     else:

@@ -28,7 +28,8 @@ __all__ = [
 ]
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_PKG, "libocs_gb300.so")
+# OCS_LIBRARY selects another build of the runner (e.g. a tuning variant)
+LIB_PATH = os.environ.get("OCS_LIBRARY") or os.path.join(_PKG, "libocs_gb300.so")
 
 # STFTProxy's default option string (StandAlone/include/STFTProxy.hpp:62)
 DEFAULT_OPTIONS = "--hanning_window --remove_dc --half_complex_return"

@@ -15,6 +15,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -61,11 +63,14 @@ struct Context {
     int device = -1;
     int sms = 0;
     cudaStream_t s_setup = nullptr;
-    std::map<int, float2*> twiddles;                             // exp -> table
+    std::map<int, float2*> twiddles;                             // exp * 2 + paired -> table
     std::map<std::tuple<int, int, uint32_t>, float*> windows;    // (kind, exp, sigma bits) -> table
-    std::map<std::pair<int, int>, int> occupancy;                // (exp, vec2) -> CTAs per SM
+    std::map<std::pair<int, int>, int> occupancy;                // (exp, output kind) -> CTAs per SM
     std::vector<Slot*> free_slots;
     std::vector<Slot*> all_slots;
+    std::map<std::tuple<int, int, int, int>, int> tuned;          // (exp, outk, dense, log2 frames) -> variant
+    bool tune_loaded = false;
+    std::string gpu_name;
 };
 
 Context& ctx()
@@ -88,6 +93,7 @@ int init_locked(Context& c, int device)
     if (p.major < 10) return fail(OCS_EINVAL, "this runner is built for sm_103a (Blackwell Ultra)");
     c.device = device;
     c.sms = p.multiProcessorCount;
+    c.gpu_name = p.name;
     OCS_CUDA(cudaStreamCreateWithFlags(&c.s_setup, cudaStreamNonBlocking));
     c.ready = true;
     return OCS_OK;
@@ -100,40 +106,46 @@ int ensure_init()
     return init_locked(c, c.ready ? c.device : -1);
 }
 
-int get_twiddles(int exp, const float2** out)
+int get_twiddles(int exp, bool paired, const float2** out)
 {
     Context& c = ctx();
     std::lock_guard<std::mutex> lk(c.mu);
-    auto it = c.twiddles.find(exp);
+    const int key = exp * 2 + (paired ? 1 : 0);
+    auto it = c.twiddles.find(key);
     if (it != c.twiddles.end()) {
         *out = it->second;
         return OCS_OK;
     }
     float2* d = nullptr;
-    const int n = ocs::fused_twiddle_count(exp);
+    const int n = paired ? ocs::pair_twiddle_count(exp) : ocs::fused_twiddle_count(exp);
     OCS_CUDA(cudaMalloc(&d, sizeof(float2) * n));
-    OCS_CUDA(ocs::build_twiddles(d, exp, c.s_setup));
+    OCS_CUDA(paired ? ocs::build_pair_twiddles(d, exp, c.s_setup) : ocs::build_twiddles(d, exp, c.s_setup));
     OCS_CUDA(cudaStreamSynchronize(c.s_setup));
-    c.twiddles[exp] = d;
+    c.twiddles[key] = d;
     *out = d;
     return OCS_OK;
 }
 
-int get_window(int kind, int exp, float sigma, const float** out)
+// Window table of (kind, exp, sigma).  scaled = true gives the table the fused
+// kernels consume: coefficients times 1/2 (exact), all 1/2 for no window.
+int get_window(int kind, int exp, float sigma, bool scaled, const float** out)
 {
     *out = nullptr;
-    if (kind == ocs::WIN_NONE) return OCS_OK;
+    if (kind == ocs::WIN_NONE && !scaled) return OCS_OK;
     Context& c = ctx();
     std::lock_guard<std::mutex> lk(c.mu);
     uint32_t sbits = 0;
     if (kind == ocs::WIN_GAUSSIAN) std::memcpy(&sbits, &sigma, 4);
-    const auto key = std::make_tuple(kind, exp, sbits);
+    const auto key = std::make_tuple(kind * 2 + (scaled ? 1 : 0), exp, sbits);
     auto it = c.windows.find(key);
     if (it != c.windows.end()) {
         *out = it->second;
         return OCS_OK;
     }
-    const std::vector<float> w = ocs::window_table(kind, 1 << exp, sigma);
+    std::vector<float> w = ocs::window_table(kind, 1 << exp, sigma);
+    if (kind == ocs::WIN_NONE) w.assign((size_t)1 << exp, 1.0f);
+    if (scaled)
+        for (float& v : w) v *= 0.5f;
     float* d = nullptr;
     OCS_CUDA(cudaMalloc(&d, sizeof(float) * w.size()));
     OCS_CUDA(cudaMemcpyAsync(d, w.data(), sizeof(float) * w.size(), cudaMemcpyHostToDevice, c.s_setup));
@@ -143,22 +155,89 @@ int get_window(int kind, int exp, float sigma, const float** out)
     return OCS_OK;
 }
 
-int grid_size(int exp, bool vec2, uint64_t frames)
+// ---------------------------------------------------------------- kernel choice
+// Variants of the fused kernel: 0 one frame per FFT, direct I/O; 1 one frame
+// per FFT, shared-memory staged I/O (windows <= 2^9); 2 two frames per FFT.
+enum { VAR_DIRECT = 0, VAR_STAGED = 1, VAR_PAIR = 2 };
+
+bool env_is(const char* name, const char* val)
+{
+    const char* e = std::getenv(name);
+    return e && std::strcmp(e, val) == 0;
+}
+
+// defaults measured on GB300 (1e8 samples, overlap 0.5) for when tuning is off
+int default_variant(int exp, int outk)
+{
+    const bool power = outk != ocs::OUT_HALF;
+    if (exp == 6) return VAR_STAGED;
+    if (power && (exp == 9 || exp == 13 || exp == 14)) return VAR_PAIR;
+    if (!power && (exp == 13 || exp == 14)) return VAR_PAIR;
+    return VAR_DIRECT;
+}
+
+bool variant_ok(int v, int exp, int outk, bool out16)
+{
+    if (v == VAR_PAIR) return ocs::pair_has(exp) && outk != ocs::OUT_PLANES && !env_is("OCS_KERNEL", "single");
+    if (v == VAR_STAGED)
+        return ocs::fused_has_staged(exp) && outk != ocs::OUT_PLANES && out16 && !env_is("OCS_IO_SCHEME", "direct");
+    return true;
+}
+
+std::string tune_cache_path()
+{
+    const char* e = std::getenv("OCS_TUNE_CACHE");
+    return e ? std::string(e) : std::string();
+}
+
+// tuning cache file: one "gpu|exp|outk|dense|bucket|variant" line per entry
+void tune_load_locked(Context& c)
+{
+    if (c.tune_loaded) return;
+    c.tune_loaded = true;
+    const std::string path = tune_cache_path();
+    if (path.empty()) return;
+    FILE* f = std::fopen(path.c_str(), "r");
+    if (!f) return;
+    char line[512];
+    while (std::fgets(line, sizeof line, f)) {
+        char name[256];
+        int e, o, d, b, v;
+        if (std::sscanf(line, "%255[^|]|%d|%d|%d|%d|%d", name, &e, &o, &d, &b, &v) == 6 && c.gpu_name == name)
+            c.tuned[std::make_tuple(e, o, d, b)] = v;
+    }
+    std::fclose(f);
+}
+
+void tune_store_locked(Context& c, const std::tuple<int, int, int, int>& k, int v)
+{
+    c.tuned[k] = v;
+    const std::string path = tune_cache_path();
+    if (path.empty()) return;
+    FILE* f = std::fopen(path.c_str(), "a");
+    if (!f) return;
+    std::fprintf(f, "%s|%d|%d|%d|%d|%d\n", c.gpu_name.c_str(), std::get<0>(k), std::get<1>(k), std::get<2>(k),
+                 std::get<3>(k), v);
+    std::fclose(f);
+}
+
+int grid_size(int exp, int outk, int variant, uint64_t frames)
 {
     Context& c = ctx();
     int occ;
     {
         std::lock_guard<std::mutex> lk(c.mu);
-        auto key = std::make_pair(exp, (int)vec2);
+        auto key = std::make_pair(exp, outk * 4 + variant);
         auto it = c.occupancy.find(key);
         if (it == c.occupancy.end()) {
-            occ = std::max(1, ocs::fused_occupancy(exp, vec2));
+            occ = std::max(1, variant == 2 ? ocs::pair_occupancy(exp, outk)
+                                           : ocs::fused_occupancy(exp, outk, variant == 1));
             c.occupancy[key] = occ;
         } else {
             occ = it->second;
         }
     }
-    const uint64_t fpc = (uint64_t)ocs::fused_frames_per_cta(exp);
+    const uint64_t fpc = (uint64_t)(variant == VAR_PAIR ? 2 * ocs::pair_per_cta(exp) : ocs::fused_frames_per_cta(exp));
     const uint64_t need = (frames + fpc - 1) / fpc;
     const uint64_t full = (uint64_t)c.sms * occ;
     return (int)std::max<uint64_t>(1, std::min(need, full));
@@ -180,15 +259,44 @@ int prepare(uint64_t n, int exp, float ov, const char* options, Request& r)
     return OCS_OK;
 }
 
-// Launch the fused kernel for frames [f0, f1) of a request.
+cudaError_t launch_variant(int v, const Request& r, int outk, ocs::FusedArgs a, const float2* tw_single,
+                           const float2* tw_pair, cudaStream_t st)
+{
+    if (v == VAR_PAIR) {
+        a.tw = tw_pair;
+        return ocs::launch_pair(r.exp, outk, a, grid_size(r.exp, outk, VAR_PAIR, a.frames), st);
+    }
+    a.tw = tw_single;
+    return ocs::launch_fused(r.exp, outk, v == VAR_STAGED, a, grid_size(r.exp, outk, v, a.frames), st);
+}
+
+int ilog2u(uint64_t v)
+{
+    int l = 0;
+    while (v > 1) {
+        v >>= 1;
+        ++l;
+    }
+    return l;
+}
+
+// Launch the fused kernel for frames [f0, f1) of a request.  The first launch
+// of a new (window, output kind, layout, size class) measures every kernel
+// variant that applies on the request's own buffers and keeps the fastest
+// (OCS_AUTOTUNE=0 disables this; OCS_TUNE_CACHE=<file> persists choices).
 int launch_frames(const Request& r, const float* d_sig, uint64_t n, float* d_out, uint64_t f0, uint64_t f1,
                   cudaStream_t st)
 {
-    const float2* tw = nullptr;
+    const float2* tw_single = nullptr;
+    const float2* tw_pair = nullptr;
     const float* win = nullptr;
-    int rc = get_twiddles(r.exp, &tw);
+    int rc = get_twiddles(r.exp, false, &tw_single);
     if (rc) return rc;
-    rc = get_window(r.opt.window, r.exp, r.opt.sigma, &win);
+    if (ocs::pair_has(r.exp)) {
+        rc = get_twiddles(r.exp, true, &tw_pair);
+        if (rc) return rc;
+    }
+    rc = get_window(r.opt.window, r.exp, r.opt.sigma, true, &win);
     if (rc) return rc;
     const uint64_t N = r.geo.n_window;
     const uint64_t hop = r.geo.hop;
@@ -199,10 +307,8 @@ int launch_frames(const Request& r, const float* d_sig, uint64_t n, float* d_out
     a.hop = hop;
     a.frames = f1 - f0;
     a.win = win;
-    a.tw = tw;
-    a.mode = r.opt.half_complex ? ocs::OCS_MODE_HALF_COMPLEX : ocs::OCS_MODE_POWER;
+    const int outk = r.opt.half_complex ? ocs::OUT_HALF : (r.opt.serial_power ? ocs::OUT_POWER_SERIAL : ocs::OUT_POWER);
     a.dense = r.opt.dense;
-    a.serial_power = r.opt.serial_power;
     a.remove_dc = r.opt.remove_dc;
     if (r.opt.dense) {
         const uint64_t row = (N / 2 + 1) * (r.opt.half_complex ? 2 : 1);
@@ -221,9 +327,64 @@ int launch_frames(const Request& r, const float* d_sig, uint64_t n, float* d_out
         a.x = d_sig;
         a.n = 0;
     }
-    const bool vec2 = (hop % 2 == 0) && ((reinterpret_cast<uintptr_t>(a.x) & 7u) == 0);
-    const int grid = grid_size(r.exp, vec2, a.frames);
-    OCS_CUDA(ocs::launch_fused(r.exp, vec2, a, grid, st));
+    const uintptr_t xa = reinterpret_cast<uintptr_t>(a.x);
+    a.vec2 = (hop % 2 == 0) && ((xa & 7u) == 0);
+    a.cs = ((hop % 4 == 0) && (xa & 15u) == 0) ? 16 : (a.vec2 ? 8 : 4);
+    const bool out16 = (reinterpret_cast<uintptr_t>(a.out) & 15u) == 0;
+
+    int cand[3], nc = 0;
+    for (int v = 0; v < 3; ++v)
+        if (variant_ok(v, r.exp, outk, out16)) cand[nc++] = v;
+    int choice = default_variant(r.exp, outk);
+    bool have = false;
+    for (int i = 0; i < nc; ++i) have |= cand[i] == choice;
+    if (!have) choice = cand[0];
+
+    const auto key = std::make_tuple(r.exp, outk, (int)r.opt.dense, ilog2u(a.frames));
+    bool need_tune = false;
+    if (nc > 1 && !env_is("OCS_AUTOTUNE", "0")) {
+        Context& c = ctx();
+        std::lock_guard<std::mutex> lk(c.mu);
+        tune_load_locked(c);
+        auto it = c.tuned.find(key);
+        if (it != c.tuned.end()) {
+            bool ok = false;
+            for (int i = 0; i < nc; ++i) ok |= cand[i] == it->second;
+            if (ok) choice = it->second;
+        } else {
+            need_tune = true;
+        }
+    }
+    if (need_tune) {
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(st, &cap);
+        if (cap == cudaStreamCaptureStatusNone) {
+            cudaEvent_t e0, e1;
+            OCS_CUDA(cudaEventCreate(&e0));
+            OCS_CUDA(cudaEventCreate(&e1));
+            float best = 1e30f;
+            for (int i = 0; i < nc; ++i) {
+                const int v = cand[i];
+                OCS_CUDA(launch_variant(v, r, outk, a, tw_single, tw_pair, st));
+                OCS_CUDA(cudaEventRecord(e0, st));
+                for (int k = 0; k < 3; ++k) OCS_CUDA(launch_variant(v, r, outk, a, tw_single, tw_pair, st));
+                OCS_CUDA(cudaEventRecord(e1, st));
+                OCS_CUDA(cudaEventSynchronize(e1));
+                float ms = 0.0f;
+                OCS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                if (ms < best) {
+                    best = ms;
+                    choice = v;
+                }
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            Context& c = ctx();
+            std::lock_guard<std::mutex> lk(c.mu);
+            tune_store_locked(c, key, choice);
+        }
+    }
+    OCS_CUDA(launch_variant(choice, r, outk, a, tw_single, tw_pair, st));
     return OCS_OK;
 }
 
@@ -481,7 +642,7 @@ int ocs_stage_window(int kind, float* d_data, uint32_t ofull, uint32_t window_si
     int rc = ensure_init();
     if (rc) return rc;
     const float* w = nullptr;
-    rc = get_window(kind, exp, sigma, &w);
+    rc = get_window(kind, exp, sigma, false, &w);
     if (rc) return rc;
     OCS_CUDA(ocs::launch_apply_window(d_data, w, ofull, window_size, (cudaStream_t)stream));
     return OCS_OK;
@@ -505,7 +666,10 @@ int ocs_stage_fft(float* d_real, float* d_imag, uint32_t ohalf, uint32_t exp, vo
     int rc = ensure_init();
     if (rc) return rc;
     const float2* tw = nullptr;
-    rc = get_twiddles((int)exp, &tw);
+    rc = get_twiddles((int)exp, false, &tw);
+    if (rc) return rc;
+    const float* half = nullptr;  // all-1/2 table: the untangle's scale, no window
+    rc = get_window(ocs::WIN_NONE, (int)exp, -1.0f, true, &half);
     if (rc) return rc;
     const uint64_t N = 1ull << exp;
     ocs::FusedArgs a{};
@@ -513,14 +677,14 @@ int ocs_stage_fft(float* d_real, float* d_imag, uint32_t ohalf, uint32_t exp, vo
     a.n = 2ull * ohalf;
     a.hop = N;
     a.frames = 2ull * ohalf / N;
-    a.win = nullptr;
+    a.win = half;
     a.tw = tw;
     a.out = d_real;
     a.out_im = d_imag;
-    a.mode = ocs::OCS_MODE_PLANES;
+    a.vec2 = (reinterpret_cast<uintptr_t>(d_real) & 7u) == 0;
     if (a.frames == 0) return OCS_OK;
-    const bool vec2 = (reinterpret_cast<uintptr_t>(d_real) & 7u) == 0;
-    OCS_CUDA(ocs::launch_fused((int)exp, vec2, a, grid_size((int)exp, vec2, a.frames), (cudaStream_t)stream));
+    OCS_CUDA(ocs::launch_fused((int)exp, ocs::OUT_PLANES, false, a,
+                               grid_size((int)exp, ocs::OUT_PLANES, VAR_DIRECT, a.frames), (cudaStream_t)stream));
     return OCS_OK;
 }
 

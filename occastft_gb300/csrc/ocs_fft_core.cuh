@@ -25,13 +25,25 @@ struct FusedCfg {
     int radix[6];
 };
 
+// Values per thread by window exponent (index 6..15); 32 values per thread
+// give one shared-memory exchange up to 2^11 at the cost of registers.
+#ifndef OCS_R_TABLE
+#define OCS_R_TABLE {16, 8, 16, 16, 16, 32, 16, 16, 16, 32}
+#endif
+__host__ __device__ constexpr int fused_R(int exp)
+{
+    constexpr int tab[10] = OCS_R_TABLE;
+    return (exp >= 6 && exp <= 15) ? tab[exp - 6] : 16;
+}
+
 __host__ __device__ constexpr FusedCfg fused_cfg(int exp)
 {
-    // M = 2^(exp-1) complex points; radix-16 stages plus one remainder stage
-    FusedCfg c{exp, exp >= 15 ? 32 : 16, 0, {1, 1, 1, 1, 1, 1}};
+    // M = 2^(exp-1) complex points; stages of radix R (<= 32) plus one remainder stage
+    FusedCfg c{exp, fused_R(exp) < (1 << (exp - 1)) ? fused_R(exp) : (1 << (exp - 1)), 0, {1, 1, 1, 1, 1, 1}};
+    const int lr = c.R == 32 ? 5 : (c.R == 16 ? 4 : (c.R == 8 ? 3 : (c.R == 4 ? 2 : 1)));
     int left = exp - 1;  // log2 M
     int s = 0;
-    while (left >= 4) { c.radix[s++] = 16; left -= 4; }
+    while (left >= lr) { c.radix[s++] = 1 << lr; left -= lr; }
     if (left > 0) c.radix[s++] = 1 << left;
     c.nstages = s;
     return c;
@@ -61,7 +73,7 @@ __host__ __device__ constexpr int fused_tw_size(int exp) { return fused_tw_offse
 __host__ __device__ constexpr int fused_cta_threads(int exp) { return fused_T(exp) >= 256 ? fused_T(exp) : 256; }
 __host__ __device__ constexpr int fused_fpc(int exp) { return fused_cta_threads(exp) / fused_T(exp); }
 // shared-memory exchange buffer per frame, in float2, padded one slot per 16
-__host__ __device__ constexpr int fused_buf_stride(int exp) { return fused_M(exp) + fused_M(exp) / 16; }
+__host__ __device__ constexpr int fused_buf_stride(int exp) { return fused_M(exp) + fused_M(exp) / fused_cfg(exp).R + 1; }
 
 // ------------------------------------------------------------------ math
 // compile-time cos/sin of 2*pi*j/L by Taylor series (for in-register DFT constants)

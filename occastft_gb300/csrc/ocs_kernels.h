@@ -6,10 +6,12 @@
 
 namespace ocs {
 
+// output kinds of the fused kernel (compile-time specialisations)
 enum : int {
-    OCS_MODE_POWER = 0,         // |X| (or the Serial runner's sqrt(2)|Re X|)
-    OCS_MODE_HALF_COMPLEX = 1,  // interleaved (re, im)
-    OCS_MODE_PLANES = 2         // separate real / imaginary planes, N bins per frame
+    OUT_POWER = 0,         // |X|, the reference's toPower kernel
+    OUT_POWER_SERIAL = 1,  // sqrt(2)|Re X|, what the reference's Serial/OpenMP runners return
+    OUT_HALF = 2,          // interleaved (re, im)
+    OUT_PLANES = 3         // separate real / imaginary planes, N bins per frame
 };
 
 struct FusedArgs {
@@ -17,24 +19,33 @@ struct FusedArgs {
     uint64_t n;            // samples readable at x
     uint64_t hop;          // frame advance in samples
     uint64_t frames;       // frames to compute
-    const float* win;      // window table (N floats) or nullptr
+    const float* win;      // window table scaled by 1/2 (N floats), never null
     const float2* tw;      // twiddle table of the plan
     float* out;            // output (or real plane)
     float* out_im;         // imaginary plane (planes mode)
     uint64_t ohalf;        // compat half-complex: number of complex outputs
-    int mode;              // OCS_MODE_*
     int dense;             // N/2+1 bins per frame instead of the reference's N
-    int serial_power;      // sqrt(2)|Re X| as the Serial runner returns
     int remove_dc;
+    int vec2;              // x + f*hop is 8-byte aligned for every frame
+    int cs;                // staged kernel: bytes per async copy (16, 8 or 4)
 };
 
 // fused single-pass STFT (windows 2^6 .. 2^15)
-cudaError_t launch_fused(int exp, bool vec2, const FusedArgs& a, int grid, cudaStream_t st);
-int fused_occupancy(int exp, bool vec2);
+cudaError_t launch_fused(int exp, int outk, bool staged, const FusedArgs& a, int grid, cudaStream_t st);
+int fused_occupancy(int exp, int outk, bool staged);
+bool fused_has_staged(int exp);
 int fused_frames_per_cta(int exp);
 int fused_twiddle_count(int exp);
 size_t fused_smem_bytes(int exp);
 cudaError_t build_twiddles(float2* tw, int exp, cudaStream_t st);
+
+// paired-frame fused STFT (two real frames per complex FFT), windows 2^6 .. 2^14
+bool pair_has(int exp);
+cudaError_t launch_pair(int exp, int outk, const FusedArgs& a, int grid, cudaStream_t st);
+int pair_occupancy(int exp, int outk);
+int pair_per_cta(int exp);
+int pair_twiddle_count(int exp);
+cudaError_t build_pair_twiddles(float2* tw, int exp, cudaStream_t st);
 
 // unfused per-stage kernels behind the runnerFunction hooks
 cudaError_t launch_overlap(const float* in, uint32_t ofull, uint32_t n, uint32_t exp, uint32_t hop,

@@ -1,0 +1,377 @@
+// Paired-frame fused STFT kernel (windows 2^6 .. 2^14, sm_103a).
+//
+// Two consecutive real frames a = 2p and b = 2p+1 ride in one N-point complex
+// FFT, z[c] = y_a[c] + i y_b[c] (the classic "two real FFTs for one" identity):
+//   A[k] = (Z[k] + conj Z[N-k]) / 2,   B[k] = (Z[k] - conj Z[N-k]) / (2i).
+// Compared with one N/2-point FFT per frame plus the real-input untangle this
+// needs no untangle twiddles, reads each window coefficient once for two
+// frames, and with 32 values per thread needs a single shared-memory exchange
+// up to N = 1024.  The 1/2 factors are folded into the window table (the
+// table is pre-scaled by 1/2, an exact operation).
+//
+// Per frame it implements the same pipeline as the reference's
+// Overlap_Common -> Window_* -> DCRemove_Common -> Stockham FFT -> toPower /
+// toHalfComplexFormat (OKL/EXPCommon.okl:7-245, OKL/kernel.okl:178-218).
+#pragma once
+#include "stft_fused_kernel.cuh"
+
+namespace ocs {
+
+// ------------------------------------------------------------ plan
+__host__ __device__ constexpr int pair_R(int exp) { return exp <= 6 ? 16 : 32; }
+
+__host__ __device__ constexpr FusedCfg pair_cfg(int exp)
+{
+    FusedCfg c{exp, pair_R(exp), 0, {1, 1, 1, 1, 1, 1}};
+    const int lr = c.R == 32 ? 5 : 4;
+    int left = exp;  // log2 of the complex FFT size N
+    int s = 0;
+    while (left >= lr) { c.radix[s++] = 1 << lr; left -= lr; }
+    if (left > 0) c.radix[s++] = 1 << left;
+    c.nstages = s;
+    return c;
+}
+__host__ __device__ constexpr int pair_T(int exp) { return (1 << exp) / pair_R(exp); }
+__host__ __device__ constexpr int pair_Ns(int exp, int s)
+{
+    int ns = 1;
+    for (int i = 0; i < s; ++i) ns *= pair_cfg(exp).radix[i];
+    return ns;
+}
+// twiddle table: for each stage s >= 1, (r_s - 1) * Ns(s) entries, (m-1)*Ns + j = W_{Ns r}^{j m}
+__host__ __device__ constexpr int pair_tw_offset(int exp, int s)
+{
+    int off = 0;
+    for (int i = 1; i < s; ++i) off += (pair_cfg(exp).radix[i] - 1) * pair_Ns(exp, i);
+    return off;
+}
+__host__ __device__ constexpr int pair_tw_size(int exp)
+{
+    return pair_tw_offset(exp, pair_cfg(exp).nstages) > 0 ? pair_tw_offset(exp, pair_cfg(exp).nstages) : 1;
+}
+__host__ __device__ constexpr int pair_cta_threads(int exp) { return pair_T(exp) >= 256 ? pair_T(exp) : 256; }
+__host__ __device__ constexpr int pair_ppc(int exp) { return pair_cta_threads(exp) / pair_T(exp); }  // pairs per CTA
+__host__ __device__ constexpr int pair_buf_stride(int exp) { return (1 << exp) + (1 << exp) / pair_R(exp) + 1; }
+__host__ __device__ constexpr bool pair_tables_in_smem(int exp) { return exp <= 11; }
+__host__ __device__ constexpr bool pair_supported(int exp) { return exp >= 6 && exp <= 14; }
+__host__ __device__ constexpr size_t pair_tab_bytes(int exp)
+{
+    return pair_tables_in_smem(exp) ? (size_t)pair_tw_size(exp) * 8 + (size_t)(1 << exp) * 4 : 0;
+}
+__host__ __device__ constexpr size_t pair_smem_bytes_ct(int exp)
+{
+    return (size_t)pair_ppc(exp) * pair_buf_stride(exp) * 8 + pair_tab_bytes(exp) +
+           (size_t)(pair_cta_threads(exp) / 32) * 8 + 16;
+}
+
+template <int EXP>
+struct PairCore {
+    static constexpr FusedCfg C = pair_cfg(EXP);
+    static constexpr int N = 1 << EXP;
+    static constexpr int R = C.R;
+    static constexpr int T = N / R;
+    static constexpr int NS = C.nstages;
+    static constexpr int LP = ilog2(R);
+    static constexpr unsigned FULL = 0xffffffffu;
+    static __device__ __forceinline__ int pd(int i) { return padl<LP>(i); }
+
+    // subtract each frame's mean: frame a is the real part, frame b the imaginary part
+    static __device__ __forceinline__ void remove_dc(float2 (&v)[R], float2* red, int tid, int lp)
+    {
+        float sa = 0.0f, sb = 0.0f;
+#pragma unroll
+        for (int u = 0; u < R; ++u) {
+            sa += v[u].x;
+            sb += v[u].y;
+        }
+        if constexpr (T <= 32) {
+#pragma unroll
+            for (int o = T / 2; o > 0; o >>= 1) {
+                sa += __shfl_xor_sync(FULL, sa, o);
+                sb += __shfl_xor_sync(FULL, sb, o);
+            }
+        } else {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                sa += __shfl_xor_sync(FULL, sa, o);
+                sb += __shfl_xor_sync(FULL, sb, o);
+            }
+            constexpr int WPF = T / 32;
+            if ((tid & 31) == 0) red[tid >> 5] = make_float2(sa, sb);
+            __syncthreads();
+            sa = 0.0f;
+            sb = 0.0f;
+#pragma unroll
+            for (int w = 0; w < WPF; ++w) {
+                const float2 r = red[lp * WPF + w];
+                sa += r.x;
+                sb += r.y;
+            }
+            __syncthreads();
+        }
+        const float ma = sa * (1.0f / (float)N), mb = sb * (1.0f / (float)N);
+#pragma unroll
+        for (int u = 0; u < R; ++u) {
+            v[u].x -= ma;
+            v[u].y -= mb;
+        }
+    }
+
+    static __device__ __forceinline__ void fft(float2 (&v)[R], float2* buf, const float2* tw, int t)
+    {
+        {
+            constexpr int r = C.radix[0];
+            static_for<0, R / r>([&](auto qc) {
+                constexpr int q = decltype(qc)::value;
+                dft_inreg<R, r, q, R / r>(v);
+            });
+        }
+        static_for<1, NS>([&](auto sc) {
+            constexpr int s = decltype(sc)::value;
+            constexpr int rp = C.radix[s - 1];
+            constexpr int nsp = pair_Ns(EXP, s - 1);
+            constexpr int r = C.radix[s];
+            constexpr int ns = pair_Ns(EXP, s);
+            constexpr int toff = pair_tw_offset(EXP, s);
+            group_sync<T>();
+            static_for<0, R / rp>([&](auto qc) {
+                constexpr int q = decltype(qc)::value;
+                const int g = t + q * T;
+                const int base = (g / nsp) * nsp * rp + (g % nsp);
+                static_for<0, rp>([&](auto mc) {
+                    constexpr int m = decltype(mc)::value;
+                    buf[pd(base + m * nsp)] = v[q + m * (R / rp)];
+                });
+            });
+            group_sync<T>();
+#pragma unroll
+            for (int u = 0; u < R; ++u) v[u] = buf[pd(t + u * T)];
+            static_for<0, R / r>([&](auto qc) {
+                constexpr int q = decltype(qc)::value;
+                const int j = (t + q * T) % ns;
+                static_for<1, r>([&](auto mc) {
+                    constexpr int m = decltype(mc)::value;
+                    v[q + m * (R / r)] = cmul(v[q + m * (R / r)], tw[toff + (m - 1) * ns + j]);
+                });
+                dft_inreg<R, r, q, R / r>(v);
+            });
+        });
+    }
+
+    static __device__ __forceinline__ void partners_prepare(const float2 (&v)[R], float2* buf, int t)
+    {
+        if constexpr (T > 32) {
+            group_sync<T>();
+#pragma unroll
+            for (int u = 0; u < R; ++u) buf[pd(t + u * T)] = v[u];
+            group_sync<T>();
+        }
+    }
+    // Z[N - (t + U*T)]
+    template <int U>
+    static __device__ __forceinline__ float2 partner_at(const float2 (&v)[R], const float2* buf, int t, int src)
+    {
+        if constexpr (T <= 32) {
+            float2 p;
+            p.x = __shfl_sync(FULL, v[R - 1 - U].x, src);
+            p.y = __shfl_sync(FULL, v[R - 1 - U].y, src);
+            return (t == 0) ? v[(R - U) % R] : p;
+        } else {
+            const float2 p = buf[pd((T - t) + (R - 1 - U) * T)];
+            return (t == 0) ? v[(R - U) % R] : p;
+        }
+    }
+    static __device__ __forceinline__ int partner_lane(int tid, int t)
+    {
+        const int lane = tid & 31;
+        return (lane & ~(T - 1)) | ((T - t) & (T - 1));
+    }
+};
+
+template <int EXP>
+__device__ __forceinline__ void pair_tables(const FusedArgs& a, float2* s_tab, int tid, const float2*& tw,
+                                            const float*& win)
+{
+    constexpr int TWN = pair_tw_size(EXP);
+    constexpr int N = 1 << EXP;
+    if constexpr (pair_tables_in_smem(EXP)) {
+        for (int i = tid; i < TWN; i += blockDim.x) s_tab[i] = a.tw[i];
+        float* sw = reinterpret_cast<float*>(s_tab + TWN);
+        for (int i = tid; i < N; i += blockDim.x) sw[i] = a.win[i];
+        __syncthreads();
+        tw = s_tab;
+        win = sw;
+    } else {
+        tw = a.tw;
+        win = a.win;
+    }
+}
+
+template <int EXP, int OUTK>
+__global__ void __launch_bounds__(pair_cta_threads(EXP), (pair_cta_threads(EXP) >= 512 ? 1 : 512 / pair_cta_threads(EXP)))
+stft_pair_kernel(const FusedArgs a)
+{
+    using K = PairCore<EXP>;
+    constexpr int N = K::N, R = K::R, T = K::T;
+    constexpr int H = N / 2;
+    constexpr int PPC = pair_ppc(EXP);
+    constexpr int BS = pair_buf_stride(EXP);
+
+    extern __shared__ float2 smem[];
+    const int tid = threadIdx.x;
+    const int lp = tid / T;
+    const int t = tid - lp * T;
+    float2* buf = smem + lp * BS;
+    float2* s_tab = smem + PPC * BS;
+    float2* red = reinterpret_cast<float2*>(reinterpret_cast<char*>(s_tab) + pair_tab_bytes(EXP));
+    const float2* tw;
+    const float* win;
+    pair_tables<EXP>(a, s_tab, tid, tw, win);
+
+    const uint64_t pairs = (a.frames + 1) / 2;
+    for (uint64_t pbase = (uint64_t)blockIdx.x * PPC; pbase < pairs; pbase += (uint64_t)gridDim.x * PPC) {
+        const uint64_t p = pbase + lp;
+        const uint64_t fa = 2 * p, fb = 2 * p + 1;
+        const bool act_a = fa < a.frames;
+        const bool act_b = fb < a.frames;
+        float2 v[R];
+
+        // ---------------- framing + window of both frames
+        {
+            const uint64_t sa = fa * a.hop;
+            const uint64_t sb = sa + a.hop;
+            const float* xa = a.x + sa;
+            const float* xb = a.x + sb;
+            if (act_b && sb + N <= a.n) {
+#pragma unroll
+                for (int u = 0; u < R; ++u) {
+                    const int c = t + u * T;
+                    v[u] = make_float2(xa[c], xb[c]);
+                }
+            } else {
+#pragma unroll
+                for (int u = 0; u < R; ++u) {
+                    const int c = t + u * T;
+                    const float ra = (act_a && sa + c < a.n) ? xa[c] : 0.0f;
+                    const float rb = (act_b && sb + c < a.n) ? xb[c] : 0.0f;
+                    v[u] = make_float2(ra, rb);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < R; ++u) {
+                const float w = win[t + u * T];
+                v[u].x *= w;
+                v[u].y *= w;
+            }
+        }
+        if (a.remove_dc) K::remove_dc(v, red, tid, lp);
+        K::fft(v, buf, tw, t);
+        K::partners_prepare(v, buf, t);
+        const int src = K::partner_lane(tid, t);
+
+        // ---------------- separate the two spectra and store
+        // slots u < R/2 carry k = t + u*T < N/2; thread 0 also owns k = N/2 (slot R/2)
+        static_for<0, R / 2 + 1>([&](auto uc) {
+            constexpr int u = decltype(uc)::value;
+            const float2 pz = K::template partner_at<u>(v, buf, t, src);
+            if (u == R / 2 && t != 0) return;
+            const int k = t + u * T;
+            const float2 z = v[u];
+            const float2 A = make_float2(z.x + pz.x, z.y - pz.y);  // frame a, bin k
+            const float2 B = make_float2(z.y + pz.y, pz.x - z.x);  // frame b, bin k
+            if constexpr (OUTK == OUT_POWER || OUTK == OUT_POWER_SERIAL) {
+                const float pa = power_of<OUTK>(A);
+                const float pb = power_of<OUTK>(B);
+                if (!a.dense) {
+                    float* ra = a.out + fa * (uint64_t)N;
+                    if (act_a) {
+                        __stcs(ra + k, pa);
+                        if (k != 0 && k != H) __stcs(ra + (N - k), pa);
+                    }
+                    if (act_b) {
+                        __stcs(ra + N + k, pb);
+                        if (k != 0 && k != H) __stcs(ra + N + (N - k), pb);
+                    }
+                } else {
+                    float* ra = a.out + fa * (uint64_t)(H + 1);
+                    if (act_a) __stcs(ra + k, pa);
+                    if (act_b) __stcs(ra + (H + 1) + k, pb);
+                }
+            } else if constexpr (OUTK == OUT_HALF) {
+                float2* o2 = reinterpret_cast<float2*>(a.out);
+                if (!a.dense) {
+                    const uint64_t fla = fa * (uint64_t)N;
+                    const uint64_t flb = fla + N;
+                    if (act_a && fla + k < a.ohalf) __stcs(o2 + fla + k, A);
+                    if (act_a && k != 0 && k != H && fla + (N - k) < a.ohalf)
+                        __stcs(o2 + fla + (N - k), make_float2(A.x, -A.y));
+                    if (act_b && flb + k < a.ohalf) __stcs(o2 + flb + k, B);
+                    if (act_b && k != 0 && k != H && flb + (N - k) < a.ohalf)
+                        __stcs(o2 + flb + (N - k), make_float2(B.x, -B.y));
+                } else {
+                    float2* ra = o2 + fa * (uint64_t)(H + 1);
+                    if (act_a) __stcs(ra + k, A);
+                    if (act_b) __stcs(ra + (H + 1) + k, B);
+                }
+            }
+        });
+    }
+}
+
+template <int EXP, int OUTK>
+cudaError_t launch_pair_t(const FusedArgs& a, int grid, cudaStream_t st)
+{
+    if constexpr (pair_supported(EXP) && OUTK != OUT_PLANES) {
+        constexpr int threads = pair_cta_threads(EXP);
+        constexpr size_t sm = pair_smem_bytes_ct(EXP);
+        auto k = stft_pair_kernel<EXP, OUTK>;
+        static bool attr_set = false;  // setting the attribute twice is harmless
+        if (!attr_set) {
+            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            if (e != cudaSuccess) return e;
+            attr_set = true;
+        }
+        k<<<grid, threads, sm, st>>>(a);
+        return cudaGetLastError();
+    } else {
+        return cudaErrorInvalidValue;
+    }
+}
+
+template <int EXP, int OUTK>
+int occupancy_pair_t()
+{
+    int blocks = 0;
+    if constexpr (pair_supported(EXP) && OUTK != OUT_PLANES) {
+        auto k = stft_pair_kernel<EXP, OUTK>;
+        constexpr size_t sm = pair_smem_bytes_ct(EXP);
+        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) return 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k, pair_cta_threads(EXP), sm) != cudaSuccess)
+            return 0;
+    }
+    return blocks;
+}
+
+template <int EXP>
+cudaError_t launch_pair_exp(int outk, const FusedArgs& a, int grid, cudaStream_t st)
+{
+    switch (outk) {
+    case OUT_POWER: return launch_pair_t<EXP, OUT_POWER>(a, grid, st);
+    case OUT_POWER_SERIAL: return launch_pair_t<EXP, OUT_POWER_SERIAL>(a, grid, st);
+    case OUT_HALF: return launch_pair_t<EXP, OUT_HALF>(a, grid, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int EXP>
+int occupancy_pair_exp(int outk)
+{
+    switch (outk) {
+    case OUT_POWER: return occupancy_pair_t<EXP, OUT_POWER>();
+    case OUT_POWER_SERIAL: return occupancy_pair_t<EXP, OUT_POWER_SERIAL>();
+    case OUT_HALF: return occupancy_pair_t<EXP, OUT_HALF>();
+    default: return 0;
+    }
+}
+
+}  // namespace ocs
