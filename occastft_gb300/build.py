@@ -78,7 +78,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         objs.append(o)
         if force or _stale(o, [s] + headers):
             jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", *inc, "-c", s, "-o", o])
-    runner_srcs = [os.path.join(RUNNER, f) for f in ("RunnerGB300.cpp", "functionImpl.cpp")]
+    runner_srcs = [os.path.join(RUNNER, f) for f in ("RunnerGB300.cpp", "functionImpl.cpp", "RunnerStandalone.cpp")]
     runner_objs = []
     for s in runner_srcs:
         if not os.path.exists(s):
@@ -97,14 +97,15 @@ def build(verbose: bool = False, force: bool = False) -> str:
     if force or jobs or not os.path.exists(LIB):
         _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-Xlinker", "-soname=libocs_gb300.so",
               "-cudart", "static", "-lpthread"])
-    if runner_objs and (force or jobs or not os.path.exists(RUNNER_LIB)):
+    if runner_objs and (force or jobs or not os.path.exists(RUNNER_LIB) or not os.path.exists(RUNNER_DEMO)):
         # the C++ Runner (reference contract) on top of the C ABI
         _run(["g++", "-shared", "-o", RUNNER_LIB, *runner_objs, "-L", PKG, "-locs_gb300",
               "-Wl,-rpath,$ORIGIN"])
         demo_src = os.path.join(RUNNER, "runner_demo.cpp")
         if os.path.exists(demo_src):
             _run(["g++", "-std=c++17", "-O2", *inc, "-I", RUNNER, demo_src, "-o", RUNNER_DEMO, "-L", PKG,
-                  "-locs_runner", "-locs_gb300", "-Wl,-rpath,$ORIGIN"])
+                  "-locs_runner", "-locs_gb300", "-L", libdir, "-lcudart", "-Wl,-rpath,$ORIGIN",
+                  "-Wl,-rpath," + libdir])
     if verbose:
         print("\n".join(l for l in log if l.strip()))
     return LIB
