@@ -99,6 +99,35 @@ int ocs_window_table(int kind, uint32_t window_size, float sigma, float* out);
 int ocs_host_alloc(void** ptr, size_t bytes);
 int ocs_host_free(void* ptr);
 
+/* ---- uneven batches: many requests, one persistent launch ---- */
+
+/* One request of a batch.  For ocs_batch_device `in` and `out` are device
+ * pointers.  `status` is written by the call: OCS_OK or the request's error. */
+typedef struct ocs_request {
+    const float* in;
+    uint64_t n;
+    int window_size_exp;
+    float overlap_ratio;
+    const char* options;
+    float* out;
+    uint64_t out_cap; /* floats */
+    int status;
+    int reserved;
+} ocs_request;
+
+/* Builds the plans (twiddle and window tables) these requests need and grows
+ * the batch's descriptor buffers, so that a following ocs_batch_device over
+ * requests of the same shapes allocates nothing and can be captured into a
+ * CUDA graph.  Replaces nothing in the reference (its runner handles one
+ * request at a time, RunnerCommon.cpp:69-134). */
+int ocs_batch_prepare(const ocs_request* reqs, int count);
+
+/* Runs all valid requests (windows 2^6..2^13) as tiles of one persistent
+ * kernel launch on `stream` (requests with larger windows get their own
+ * fused launch on the same stream).  Asynchronous.  Returns OCS_OK when the
+ * launch was issued; per-request problems land in reqs[i].status. */
+int ocs_batch_device(ocs_request* reqs, int count, void* stream);
+
 /* ---- per-stage hooks: runnerFunction::* (RunnerInterface.hpp:38-76) on
  * device buffers laid out as the reference's [qt][N] planes. ---- */
 

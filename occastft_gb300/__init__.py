@@ -86,6 +86,8 @@ SIGNATURES = {
     "ocs_window_table": (ctypes.c_int, [ctypes.c_int, ctypes.c_uint32, ctypes.c_float, _VP]),
     "ocs_host_alloc": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t]),
     "ocs_host_free": (ctypes.c_int, [_VP]),
+    "ocs_batch_prepare": (ctypes.c_int, [_VP, ctypes.c_int]),
+    "ocs_batch_device": (ctypes.c_int, [_VP, ctypes.c_int, _VP]),
     "ocs_stage_overlap": (ctypes.c_int, [_VP, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                          _VP, _VP]),
     "ocs_stage_window": (ctypes.c_int, [ctypes.c_int, _VP, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, _VP]),
@@ -168,6 +170,52 @@ def window_table(kind: int, window_size: int, sigma: float = -1.0) -> np.ndarray
     out = np.empty(window_size, dtype=np.float32)
     _check(lib().ocs_window_table(kind, window_size, sigma, out.ctypes.data))
     return out
+
+
+class Request(ctypes.Structure):
+    """ocs_request: one request of a batch (device pointers)."""
+
+    _fields_ = [
+        ("in_", ctypes.c_void_p),
+        ("n", ctypes.c_uint64),
+        ("window_size_exp", ctypes.c_int),
+        ("overlap_ratio", ctypes.c_float),
+        ("options", ctypes.c_char_p),
+        ("out", ctypes.c_void_p),
+        ("out_cap", ctypes.c_uint64),
+        ("status", ctypes.c_int),
+        ("reserved", ctypes.c_int),
+    ]
+
+
+def make_requests(items):
+    """items: iterable of (d_in, n, exp, overlap, options, d_out, out_cap); pointers as ints or tensors."""
+    items = list(items)
+    arr = (Request * len(items))()
+    keep = []
+    for i, (din, n, exp, ov, opts, dout, cap) in enumerate(items):
+        ob = opts.encode()
+        keep.append(ob)
+        arr[i].in_ = din.data_ptr() if hasattr(din, "data_ptr") else int(din)
+        arr[i].n = n
+        arr[i].window_size_exp = exp
+        arr[i].overlap_ratio = ov
+        arr[i].options = ob
+        arr[i].out = dout.data_ptr() if hasattr(dout, "data_ptr") else int(dout)
+        arr[i].out_cap = cap
+        arr[i].status = -1
+    arr._keep = keep  # the option strings must outlive the array
+    return arr
+
+
+def batch_prepare(reqs) -> None:
+    _check(lib().ocs_batch_prepare(ctypes.cast(reqs, ctypes.c_void_p), len(reqs)))
+
+
+def batch_device(reqs, stream=None) -> list:
+    """One persistent launch over all requests; returns the per-request status codes."""
+    _check(lib().ocs_batch_device(ctypes.cast(reqs, ctypes.c_void_p), len(reqs), _stream_handle(stream)))
+    return [r.status for r in reqs]
 
 
 class Runner:

@@ -69,6 +69,14 @@ struct Context {
     std::vector<Slot*> free_slots;
     std::vector<Slot*> all_slots;
     std::map<std::tuple<int, int, int, int>, int> tuned;          // (exp, outk, dense, log2 frames) -> variant
+    // uneven batches: descriptors staged in pinned memory, copied to device scratch
+    std::mutex batch_mu;
+    char* batch_host = nullptr;
+    size_t batch_host_cap = 0;
+    char* batch_dev = nullptr;
+    size_t batch_dev_cap = 0;
+    cudaEvent_t batch_staged = nullptr;
+    int batch_occ = 0;
     bool tune_loaded = false;
     std::string gpu_name;
 };
@@ -466,6 +474,180 @@ int grow(float** p, size_t* cap, size_t need)
 
 }  // namespace
 
+
+// ---------------------------------------------------------------- batches
+namespace {
+
+struct BatchPlan {
+    std::vector<ocs::FusedArgs> descs;   // one per request in the persistent launch
+    std::vector<ocs::BatchTile> tiles;
+    std::vector<int> big;                // requests with windows above the batch kernel's range
+    std::vector<Request> parsed;
+};
+
+size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+// Parses every request, builds plans, descriptors and the ordered tile list.
+int batch_build(ocs_request* reqs, int count, BatchPlan& bp, bool write_status)
+{
+    bp.parsed.assign(count, Request{});
+    std::vector<int> order;
+    for (int i = 0; i < count; ++i) {
+        ocs_request& q = reqs[i];
+        Request& r = bp.parsed[i];
+        int rc = prepare(q.n, q.window_size_exp, q.overlap_ratio, q.options, r);
+        if (!rc && q.out_cap < r.geo.out_floats) rc = fail(OCS_ESPACE, "output buffer too small");
+        if (!rc && (!q.in || !q.out)) rc = fail(OCS_EINVAL, "null buffer");
+        if (!rc) {
+            const float2* tw = nullptr;
+            const float* win = nullptr;
+            rc = get_twiddles(r.exp, false, &tw);
+            if (!rc) rc = get_window(r.opt.window, r.exp, r.opt.sigma, true, &win);
+            if (!rc && ocs::pair_has(r.exp)) {
+                const float2* twp = nullptr;
+                rc = get_twiddles(r.exp, true, &twp);
+            }
+        }
+        if (write_status) q.status = rc;
+        if (rc) continue;
+        if (ocs::batch_supports(r.exp)) order.push_back(i);
+        else bp.big.push_back(i);
+    }
+    auto outk_of = [&](int i) {
+        const Request& r = bp.parsed[i];
+        return r.opt.half_complex ? ocs::OUT_HALF : (r.opt.serial_power ? ocs::OUT_POWER_SERIAL : ocs::OUT_POWER);
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        const int ea = bp.parsed[a].exp, eb = bp.parsed[b].exp;
+        return ea != eb ? ea < eb : outk_of(a) < outk_of(b);
+    });
+    for (int i : order) {
+        const Request& r = bp.parsed[i];
+        const ocs_request& q = reqs[i];
+        ocs::FusedArgs a{};
+        const float2* tw = nullptr;
+        const float* win = nullptr;
+        get_twiddles(r.exp, false, &tw);
+        get_window(r.opt.window, r.exp, r.opt.sigma, true, &win);
+        a.x = q.in;
+        a.n = q.n;
+        a.hop = r.geo.hop;
+        a.frames = r.geo.frames;
+        a.win = win;
+        a.tw = tw;
+        a.out = q.out;
+        a.ohalf = r.opt.half_complex && !r.opt.dense ? r.geo.ohalf : 0;
+        a.dense = r.opt.dense;
+        a.remove_dc = r.opt.remove_dc;
+        a.vec2 = (r.geo.hop % 2 == 0) && ((reinterpret_cast<uintptr_t>(q.in) & 7u) == 0);
+        a.exp = r.exp;
+        a.outk = outk_of(i);
+        const uint32_t idx = (uint32_t)bp.descs.size();
+        bp.descs.push_back(a);
+        const uint64_t tf = (uint64_t)ocs::batch_tile_frames(r.exp);
+        for (uint64_t f0 = 0; f0 < r.geo.frames; f0 += tf) {
+            ocs::BatchTile t;
+            t.req = idx;
+            t.nframes = (uint32_t)std::min<uint64_t>(tf, r.geo.frames - f0);
+            t.f0 = f0;
+            bp.tiles.push_back(t);
+        }
+    }
+    return OCS_OK;
+}
+
+size_t batch_bytes(size_t ndesc, size_t ntiles)
+{
+    return align256(ndesc * sizeof(ocs::FusedArgs)) + align256(ntiles * sizeof(ocs::BatchTile)) + 256;
+}
+
+int batch_grow_locked(Context& c, size_t bytes)
+{
+    if (c.batch_host_cap < bytes) {
+        if (c.batch_staged) OCS_CUDA(cudaEventSynchronize(c.batch_staged));
+        if (c.batch_host) cudaFreeHost(c.batch_host);
+        c.batch_host = nullptr;
+        c.batch_host_cap = 0;
+        OCS_CUDA(cudaHostAlloc((void**)&c.batch_host, bytes, cudaHostAllocPortable));
+        c.batch_host_cap = bytes;
+    }
+    if (c.batch_dev_cap < bytes) {
+        if (c.batch_dev) {
+            OCS_CUDA(cudaDeviceSynchronize());
+            cudaFree(c.batch_dev);
+        }
+        c.batch_dev = nullptr;
+        c.batch_dev_cap = 0;
+        OCS_CUDA(cudaMalloc((void**)&c.batch_dev, bytes));
+        c.batch_dev_cap = bytes;
+    }
+    if (!c.batch_staged) OCS_CUDA(cudaEventCreateWithFlags(&c.batch_staged, cudaEventDisableTiming));
+    if (!c.batch_occ) c.batch_occ = std::max(1, ocs::batch_occupancy());
+    return OCS_OK;
+}
+
+}  // namespace
+
+extern "C" int ocs_batch_prepare(const ocs_request* reqs, int count)
+{
+    if (count < 0 || (count > 0 && !reqs)) return fail(OCS_EINVAL, "bad request list");
+    int rc = ensure_init();
+    if (rc) return rc;
+    std::vector<ocs_request> copy(reqs, reqs + count);
+    BatchPlan bp;
+    rc = batch_build(copy.data(), count, bp, true);
+    if (rc) return rc;
+    Context& c = ctx();
+    std::lock_guard<std::mutex> lk(c.batch_mu);
+    return batch_grow_locked(c, batch_bytes(bp.descs.size(), bp.tiles.size()));
+}
+
+extern "C" int ocs_batch_device(ocs_request* reqs, int count, void* stream)
+{
+    if (count < 0 || (count > 0 && !reqs)) return fail(OCS_EINVAL, "bad request list");
+    int rc = ensure_init();
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    OCS_CUDA(cudaStreamIsCapturing(st, &cap));
+    const bool capturing = cap != cudaStreamCaptureStatusNone;
+    BatchPlan bp;
+    rc = batch_build(reqs, count, bp, true);
+    if (rc) return rc;
+    Context& c = ctx();
+    if (!bp.tiles.empty()) {
+        std::lock_guard<std::mutex> lk(c.batch_mu);
+        const size_t bytes = batch_bytes(bp.descs.size(), bp.tiles.size());
+        if (capturing && (c.batch_host_cap < bytes || c.batch_dev_cap < bytes))
+            return fail(OCS_ENOMEM, "batch buffers not prepared (call ocs_batch_prepare before capture)");
+        rc = batch_grow_locked(c, bytes);
+        if (rc) return rc;
+        // the previous batch's descriptors must have left the staging buffer
+        if (!capturing) OCS_CUDA(cudaEventSynchronize(c.batch_staged));
+        const size_t o_tiles = align256(bp.descs.size() * sizeof(ocs::FusedArgs));
+        const size_t o_cnt = o_tiles + align256(bp.tiles.size() * sizeof(ocs::BatchTile));
+        std::memcpy(c.batch_host, bp.descs.data(), bp.descs.size() * sizeof(ocs::FusedArgs));
+        std::memcpy(c.batch_host + o_tiles, bp.tiles.data(), bp.tiles.size() * sizeof(ocs::BatchTile));
+        const uint32_t nt = (uint32_t)bp.tiles.size();
+        std::memcpy(c.batch_host + o_cnt, &nt, 4);
+        std::memset(c.batch_host + o_cnt + 4, 0, 4);  // tile counter starts at zero
+        OCS_CUDA(cudaMemcpyAsync(c.batch_dev, c.batch_host, o_cnt + 8, cudaMemcpyHostToDevice, st));
+        if (!capturing) OCS_CUDA(cudaEventRecord(c.batch_staged, st));
+        auto* d_reqs = reinterpret_cast<const ocs::FusedArgs*>(c.batch_dev);
+        auto* d_tiles = reinterpret_cast<const ocs::BatchTile*>(c.batch_dev + o_tiles);
+        auto* d_nt = reinterpret_cast<const uint32_t*>(c.batch_dev + o_cnt);
+        auto* d_cnt = reinterpret_cast<uint32_t*>(c.batch_dev + o_cnt + 4);
+        const int grid = std::max(1, std::min<int>(c.sms * c.batch_occ, (int)bp.tiles.size()));
+        OCS_CUDA(ocs::launch_batch(d_reqs, d_tiles, d_nt, d_cnt, grid, st));
+    }
+    for (int i : bp.big) {
+        const Request& r = bp.parsed[i];
+        rc = launch_frames(r, reqs[i].in, reqs[i].n, reqs[i].out, 0, r.geo.frames, st);
+        reqs[i].status = rc;
+    }
+    return OCS_OK;
+}
+
 extern "C" {
 
 int ocs_init(int device)
@@ -499,6 +681,14 @@ void ocs_shutdown(void)
     c.all_slots.clear();
     c.free_slots.clear();
     c.occupancy.clear();
+    if (c.batch_host) cudaFreeHost(c.batch_host);
+    if (c.batch_dev) cudaFree(c.batch_dev);
+    if (c.batch_staged) cudaEventDestroy(c.batch_staged);
+    c.batch_host = nullptr;
+    c.batch_dev = nullptr;
+    c.batch_staged = nullptr;
+    c.batch_host_cap = c.batch_dev_cap = 0;
+    c.batch_occ = 0;
     if (c.s_setup) cudaStreamDestroy(c.s_setup);
     c.s_setup = nullptr;
     c.ready = false;

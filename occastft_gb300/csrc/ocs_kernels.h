@@ -11,7 +11,8 @@ enum : int {
     OUT_POWER = 0,         // |X|, the reference's toPower kernel
     OUT_POWER_SERIAL = 1,  // sqrt(2)|Re X|, what the reference's Serial/OpenMP runners return
     OUT_HALF = 2,          // interleaved (re, im)
-    OUT_PLANES = 3         // separate real / imaginary planes, N bins per frame
+    OUT_PLANES = 3,        // separate real / imaginary planes, N bins per frame
+    OUT_RUNTIME = -1       // kind read from FusedArgs::outk (batch kernel)
 };
 
 struct FusedArgs {
@@ -28,6 +29,8 @@ struct FusedArgs {
     int remove_dc;
     int vec2;              // x + f*hop is 8-byte aligned for every frame
     int cs;                // staged kernel: bytes per async copy (16, 8 or 4)
+    int exp;               // window exponent (batch kernel)
+    int outk;              // output kind (batch kernel)
 };
 
 // fused single-pass STFT (windows 2^6 .. 2^15)
@@ -46,6 +49,19 @@ int pair_occupancy(int exp, int outk);
 int pair_per_cta(int exp);
 int pair_twiddle_count(int exp);
 cudaError_t build_pair_twiddles(float2* tw, int exp, cudaStream_t st);
+
+// uneven batch: one persistent launch over a device tile queue
+struct BatchTile {
+    uint32_t req;      // index into the request descriptors
+    uint32_t nframes;  // frames in this tile
+    uint64_t f0;       // first frame
+};
+bool batch_supports(int exp);
+int batch_tile_frames(int exp);
+int batch_occupancy();
+size_t batch_smem_bytes();
+cudaError_t launch_batch(const FusedArgs* d_reqs, const BatchTile* d_tiles, const uint32_t* d_ntiles,
+                         uint32_t* d_counter, int grid, cudaStream_t st);
 
 // unfused per-stage kernels behind the runnerFunction hooks
 cudaError_t launch_overlap(const float* in, uint32_t ofull, uint32_t n, uint32_t exp, uint32_t hop,

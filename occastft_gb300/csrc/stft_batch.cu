@@ -1,0 +1,105 @@
+// Uneven batch in one persistent launch.
+//
+// Many requests (each its own signal, window exponent 2^6..2^13, overlap,
+// window kind and output layout) are cut into tiles of consecutive frames.
+// A persistent grid pulls tiles from a device queue with one atomic per tile
+// and runs the fused STFT body specialised for the tile's window size; the
+// output kind is read per request.  Tiles are ordered by (window, output
+// kind) on the host so that concurrently running CTAs mostly share one code
+// path.
+#include "stft_fused_kernel.cuh"
+
+namespace ocs {
+
+constexpr int kBatchMinExp = 6;
+constexpr int kBatchMaxExp = 13;
+
+__host__ __device__ constexpr size_t batch_group_smem(int exp)
+{
+    return (size_t)fused_fpc(exp) * fused_buf_stride(exp) * 8 + (size_t)(256 / 32) * 4 + 16;
+}
+__host__ __device__ constexpr size_t batch_smem_ct()
+{
+    size_t m = 0;
+    for (int e = kBatchMinExp; e <= kBatchMaxExp; ++e) m = batch_group_smem(e) > m ? batch_group_smem(e) : m;
+    return m;
+}
+
+template <int EXP>
+__device__ __forceinline__ void batch_tile(const FusedArgs& a, uint64_t f0, uint32_t nf, float2* smem)
+{
+    static_assert(fused_cta_threads(EXP) == 256, "batch CTAs have 256 threads");
+    using K = Core<EXP>;
+    constexpr int T = K::T;
+    constexpr int FPC = fused_fpc(EXP);
+    constexpr int BS = fused_buf_stride(EXP);
+    const int tid = threadIdx.x;
+    const int lf = tid / T;
+    const int t = tid - lf * T;
+    float2* buf = smem + lf * BS;
+    float* red = reinterpret_cast<float*>(smem + FPC * BS);
+    FusedArgs b = a;
+    b.frames = f0 + nf;  // frames past the tile belong to the next tile
+    for (uint64_t fb = f0; fb < f0 + nf; fb += FPC)
+        fused_group_frames<EXP, OUT_RUNTIME>(b, fb, buf, red, a.tw, reinterpret_cast<const float2*>(a.win), tid, lf,
+                                             t);
+}
+
+__global__ void __launch_bounds__(256, 2)
+stft_batch_kernel(const FusedArgs* __restrict__ reqs, const BatchTile* __restrict__ tiles,
+                  const uint32_t* __restrict__ ntiles, uint32_t* __restrict__ counter)
+{
+    extern __shared__ float2 smem[];
+    __shared__ uint32_t s_tile;
+    const uint32_t nt = *ntiles;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1u);
+        __syncthreads();
+        const uint32_t ti = s_tile;
+        __syncthreads();  // every thread has read s_tile; the previous tile's smem use is over
+        if (ti >= nt) break;
+        const BatchTile tl = tiles[ti];
+        const FusedArgs a = reqs[tl.req];
+        switch (a.exp) {
+        case 6: batch_tile<6>(a, tl.f0, tl.nframes, smem); break;
+        case 7: batch_tile<7>(a, tl.f0, tl.nframes, smem); break;
+        case 8: batch_tile<8>(a, tl.f0, tl.nframes, smem); break;
+        case 9: batch_tile<9>(a, tl.f0, tl.nframes, smem); break;
+        case 10: batch_tile<10>(a, tl.f0, tl.nframes, smem); break;
+        case 11: batch_tile<11>(a, tl.f0, tl.nframes, smem); break;
+        case 12: batch_tile<12>(a, tl.f0, tl.nframes, smem); break;
+        case 13: batch_tile<13>(a, tl.f0, tl.nframes, smem); break;
+        default: break;
+        }
+    }
+}
+
+size_t batch_smem_bytes() { return batch_smem_ct(); }
+bool batch_supports(int exp) { return exp >= kBatchMinExp && exp <= kBatchMaxExp; }
+int batch_tile_frames(int exp) { return fused_fpc(exp) * 4; }
+
+int batch_occupancy()
+{
+    int blocks = 0;
+    const size_t sm = batch_smem_ct();
+    if (cudaFuncSetAttribute(stft_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+        return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, stft_batch_kernel, 256, sm) != cudaSuccess) return 0;
+    return blocks;
+}
+
+cudaError_t launch_batch(const FusedArgs* d_reqs, const BatchTile* d_tiles, const uint32_t* d_ntiles,
+                         uint32_t* d_counter, int grid, cudaStream_t st)
+{
+    static bool attr_set = false;  // setting the attribute twice is harmless
+    const size_t sm = batch_smem_ct();
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(stft_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    stft_batch_kernel<<<grid, 256, sm, st>>>(d_reqs, d_tiles, d_ntiles, d_counter);
+    return cudaGetLastError();
+}
+
+}  // namespace ocs

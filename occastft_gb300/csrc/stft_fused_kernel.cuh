@@ -272,12 +272,111 @@ __device__ __forceinline__ void load_tables(const FusedArgs& a, float2* s_tab, i
 }
 
 // ============================================================ direct I/O kernel
+// One CTA-iteration: frames [fbase + lf] for every frame group of the CTA.
+// OUTK may be OUT_RUNTIME, in which case a.outk selects the output kind
+// (the batch kernel mixes requests of different kinds).
+template <int EXP, int OUTK>
+__device__ __forceinline__ void fused_group_frames(const FusedArgs& a, uint64_t fbase, float2* buf, float* red,
+                                                   const float2* tw, const float2* win2, int tid, int lf, int t)
+{
+    using K = Core<EXP>;
+    constexpr int N = K::N, M = K::M, R = K::R, T = K::T;
+    const bool vec2 = a.vec2 != 0;
+    const int outk = OUTK == OUT_RUNTIME ? a.outk : OUTK;
+    const uint64_t f = fbase + lf;
+    const bool active = f < a.frames;
+    float2 v[R];
+
+    // ---------------- framing + window (one HBM read of the frame)
+    {
+        const uint64_t s = f * a.hop;
+        const float* xs = a.x + s;
+        if (active && s + N <= a.n) {
+            if (vec2) {
+#pragma unroll
+                for (int u = 0; u < R; ++u) v[u] = reinterpret_cast<const float2*>(xs)[t + u * T];
+            } else {
+#pragma unroll
+                for (int u = 0; u < R; ++u) {
+                    const int c = t + u * T;
+                    v[u] = make_float2(xs[2 * c], xs[2 * c + 1]);
+                }
+            }
+        } else if (active) {
+#pragma unroll
+            for (int u = 0; u < R; ++u) {
+                const uint64_t c = (uint64_t)(t + u * T);
+                const uint64_t i0 = s + 2 * c;
+                v[u] = make_float2(i0 < a.n ? xs[2 * c] : 0.0f, i0 + 1 < a.n ? xs[2 * c + 1] : 0.0f);
+            }
+        } else {
+#pragma unroll
+            for (int u = 0; u < R; ++u) v[u] = make_float2(0.0f, 0.0f);
+        }
+#pragma unroll
+        for (int u = 0; u < R; ++u) {
+            const float2 w = win2[t + u * T];
+            v[u].x *= w.x;
+            v[u].y *= w.y;
+        }
+    }
+    if (a.remove_dc) K::remove_dc(v, red, tid, lf);
+    K::fft(v, buf, tw, t);
+    K::partners_prepare(v, buf, t);
+    const int src = K::partner_lane(tid, t);
+
+    // ---------------- untangle + fused output store
+    static_for<0, R>([&](auto uc) {
+        constexpr int u = decltype(uc)::value;
+        const float2 pu = K::template partner_at<u>(v, buf, t, src);
+        if (!active) return;
+        const int k = t + u * T;
+        float2 e, wo;
+        K::untangle(v[u], pu, tw[k], e, wo);
+        const float2 xa = cadd(e, wo);  // X[k]
+        if (outk == OUT_POWER || outk == OUT_POWER_SERIAL) {
+            const bool ser = OUTK == OUT_POWER_SERIAL || (OUTK == OUT_RUNTIME && outk == OUT_POWER_SERIAL);
+            const float p = ser ? power_of<OUT_POWER_SERIAL>(xa) : power_of<OUT_POWER>(xa);
+            const float2 xb = csub(e, wo);
+            if (!a.dense) {
+                float* row = a.out + f * (uint64_t)N;
+                __stcs(row + k, p);
+                if (k != 0) __stcs(row + (N - k), p);  // |X[N-k]| = |X[k]| for real frames
+                else __stcs(row + M, ser ? power_of<OUT_POWER_SERIAL>(xb) : power_of<OUT_POWER>(xb));
+            } else {
+                float* row = a.out + f * (uint64_t)(M + 1);
+                __stcs(row + k, p);
+                if (k == 0) __stcs(row + M, ser ? power_of<OUT_POWER_SERIAL>(xb) : power_of<OUT_POWER>(xb));
+            }
+        } else if (outk == OUT_HALF) {
+            const float2 xb = csub(e, wo);  // X[k + M]
+            float2* o2 = reinterpret_cast<float2*>(a.out);
+            if (!a.dense) {
+                const uint64_t flat = f * (uint64_t)N + k;
+                if (flat < a.ohalf) __stcs(o2 + flat, xa);
+                if (flat + M < a.ohalf) __stcs(o2 + flat + M, xb);
+            } else {
+                float2* row = o2 + f * (uint64_t)(M + 1);
+                __stcs(row + k, xa);
+                if (k == 0) __stcs(row + M, xb);
+            }
+        } else {  // planes
+            const float2 xb = csub(e, wo);
+            const uint64_t b = f * (uint64_t)N + k;
+            a.out[b] = xa.x;
+            a.out_im[b] = xa.y;
+            a.out[b + M] = xb.x;
+            a.out_im[b + M] = xb.y;
+        }
+    });
+}
+
 template <int EXP, int OUTK>
 __global__ void __launch_bounds__(fused_cta_threads(EXP), (fused_cta_threads(EXP) >= 512 ? 1 : 512 / fused_cta_threads(EXP)))
 stft_fused_kernel(const FusedArgs a)
 {
     using K = Core<EXP>;
-    constexpr int N = K::N, M = K::M, R = K::R, T = K::T;
+    constexpr int T = K::T;
     constexpr int FPC = fused_fpc(EXP);
     constexpr int BS = fused_buf_stride(EXP);
 
@@ -291,94 +390,8 @@ stft_fused_kernel(const FusedArgs a)
     const float2* tw;
     const float2* win2;
     load_tables<EXP>(a, s_tab, tid, tw, win2);
-    const bool vec2 = a.vec2 != 0;
-
-    for (uint64_t fbase = (uint64_t)blockIdx.x * FPC; fbase < a.frames; fbase += (uint64_t)gridDim.x * FPC) {
-        const uint64_t f = fbase + lf;
-        const bool active = f < a.frames;
-        float2 v[R];
-
-        // ---------------- framing + window (one HBM read of the frame)
-        {
-            const uint64_t s = f * a.hop;
-            const float* xs = a.x + s;
-            if (active && s + N <= a.n) {
-                if (vec2) {
-#pragma unroll
-                    for (int u = 0; u < R; ++u) v[u] = reinterpret_cast<const float2*>(xs)[t + u * T];
-                } else {
-#pragma unroll
-                    for (int u = 0; u < R; ++u) {
-                        const int c = t + u * T;
-                        v[u] = make_float2(xs[2 * c], xs[2 * c + 1]);
-                    }
-                }
-            } else if (active) {
-#pragma unroll
-                for (int u = 0; u < R; ++u) {
-                    const uint64_t c = (uint64_t)(t + u * T);
-                    const uint64_t i0 = s + 2 * c;
-                    v[u] = make_float2(i0 < a.n ? xs[2 * c] : 0.0f, i0 + 1 < a.n ? xs[2 * c + 1] : 0.0f);
-                }
-            } else {
-#pragma unroll
-                for (int u = 0; u < R; ++u) v[u] = make_float2(0.0f, 0.0f);
-            }
-#pragma unroll
-            for (int u = 0; u < R; ++u) {
-                const float2 w = win2[t + u * T];
-                v[u].x *= w.x;
-                v[u].y *= w.y;
-            }
-        }
-        if (a.remove_dc) K::remove_dc(v, red, tid, lf);
-        K::fft(v, buf, tw, t);
-        K::partners_prepare(v, buf, t);
-        const int src = K::partner_lane(tid, t);
-
-        // ---------------- untangle + fused output store
-        static_for<0, R>([&](auto uc) {
-            constexpr int u = decltype(uc)::value;
-            const float2 pu = K::template partner_at<u>(v, buf, t, src);
-            if (!active) return;
-            const int k = t + u * T;
-            float2 e, wo;
-            K::untangle(v[u], pu, tw[k], e, wo);
-            const float2 xa = cadd(e, wo);  // X[k]
-            if constexpr (OUTK == OUT_POWER || OUTK == OUT_POWER_SERIAL) {
-                const float p = power_of<OUTK>(xa);
-                if (!a.dense) {
-                    float* row = a.out + f * (uint64_t)N;
-                    __stcs(row + k, p);
-                    if (k != 0) __stcs(row + (N - k), p);  // |X[N-k]| = |X[k]| for real frames
-                    else __stcs(row + M, power_of<OUTK>(csub(e, wo)));
-                } else {
-                    float* row = a.out + f * (uint64_t)(M + 1);
-                    __stcs(row + k, p);
-                    if (k == 0) __stcs(row + M, power_of<OUTK>(csub(e, wo)));
-                }
-            } else if constexpr (OUTK == OUT_HALF) {
-                const float2 xb = csub(e, wo);  // X[k + M]
-                float2* o2 = reinterpret_cast<float2*>(a.out);
-                if (!a.dense) {
-                    const uint64_t flat = f * (uint64_t)N + k;
-                    if (flat < a.ohalf) __stcs(o2 + flat, xa);
-                    if (flat + M < a.ohalf) __stcs(o2 + flat + M, xb);
-                } else {
-                    float2* row = o2 + f * (uint64_t)(M + 1);
-                    __stcs(row + k, xa);
-                    if (k == 0) __stcs(row + M, xb);
-                }
-            } else {  // planes
-                const float2 xb = csub(e, wo);
-                const uint64_t b = f * (uint64_t)N + k;
-                a.out[b] = xa.x;
-                a.out_im[b] = xa.y;
-                a.out[b + M] = xb.x;
-                a.out_im[b + M] = xb.y;
-            }
-        });
-    }
+    for (uint64_t fbase = (uint64_t)blockIdx.x * FPC; fbase < a.frames; fbase += (uint64_t)gridDim.x * FPC)
+        fused_group_frames<EXP, OUTK>(a, fbase, buf, red, tw, win2, tid, lf, t);
 }
 
 // ============================================================ staged I/O kernel

@@ -1,0 +1,130 @@
+"""Uneven batches in one persistent launch (C ABI ocs_batch_device):
+per-request parity with the single-request path and the FP64 oracle,
+alone-vs-in-the-mix equality, per-request errors, CUDA-graph capture."""
+import numpy as np
+import pytest
+
+from tests.conftest import signal
+
+REL_L2 = 1e-5
+pytestmark = pytest.mark.gpu
+
+WINDOWS = ["--hanning_window", "--hamming_window", "--blackman_window", "--flattop_window",
+           "--gaussian_window=x0.3<<sigma", ""]
+OUTS = ["", " --half_complex_return", " --layout=dense", " --half_complex_return --layout=dense", " --serial_power"]
+
+
+def _mix(count, seed=0, exps=range(6, 16)):
+    import torch
+
+    rng = np.random.default_rng(seed)
+    exps = list(exps)
+    items = []
+    for i in range(count):
+        exp = int(rng.choice(exps))
+        N = 1 << exp
+        n = int(rng.integers(N // 2, 12 * N))
+        ov = float(rng.choice([0.0, 0.25, 0.5, 0.75, 0.3]))
+        opts = str(rng.choice(WINDOWS)) + str(rng.choice(OUTS)) + (" --remove_dc" if rng.random() < 0.5 else "")
+        x = signal(1000 + i, n)
+        items.append((x, exp, ov, opts.strip()))
+    return items
+
+
+def _run_batch(ocs_lib, items, stream=None):
+    import torch
+
+    bufs = []
+    reqs_in = []
+    for (x, exp, ov, opts) in items:
+        g = ocs_lib.geometry(x.size, exp, ov, opts)
+        d_in = torch.from_numpy(x).cuda()
+        d_out = torch.full((g.out_floats + 8,), float("nan"), device="cuda")
+        bufs.append((d_in, d_out, g))
+        reqs_in.append((d_in, x.size, exp, ov, opts, d_out, g.out_floats))
+    reqs = ocs_lib.make_requests(reqs_in)
+    st = ocs_lib.batch_device(reqs, stream)
+    torch.cuda.synchronize()
+    return st, [b[1].cpu().numpy() for b in bufs], bufs
+
+
+def test_mixed_batch_matches_single_requests(ocs_lib, orc):
+    items = _mix(48, seed=1)
+    st, outs, bufs = _run_batch(ocs_lib, items)
+    assert all(s == 0 for s in st), st
+    for (x, exp, ov, opts), out, (_, _, g) in zip(items, outs, bufs):
+        got = out[: g.out_floats]
+        assert not np.isnan(got).any() and np.isnan(out[g.out_floats:]).all(), (exp, opts)
+        single = ocs_lib.activate(x, exp, ov, opts)
+        assert orc.rel_l2(got, single) <= REL_L2, (exp, ov, opts)
+        ref = orc.fp64_stft(x, exp, ov, opts)
+        assert orc.rel_l2(got, ref) <= REL_L2, (exp, ov, opts)
+
+
+def test_alone_equals_in_the_mix(ocs_lib):
+    items = _mix(30, seed=2, exps=range(6, 14))
+    _, mixed, _ = _run_batch(ocs_lib, items)
+    for k in (0, 7, 19, 29):
+        _, alone, _ = _run_batch(ocs_lib, [items[k]])
+        assert np.array_equal(alone[0], mixed[k], equal_nan=True), k
+
+
+def test_batch_deterministic(ocs_lib):
+    items = _mix(20, seed=3)
+    _, a, _ = _run_batch(ocs_lib, items)
+    _, b, _ = _run_batch(ocs_lib, items)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y, equal_nan=True)
+
+
+def test_per_request_errors(ocs_lib, orc):
+    import torch
+
+    x = signal(5, 5000)
+    d_in = torch.from_numpy(x).cuda()
+    g = ocs_lib.geometry(x.size, 8, 0.5, "--hanning_window")
+    outs = [torch.zeros(g.out_floats, device="cuda") for _ in range(3)]
+    reqs = ocs_lib.make_requests([
+        (d_in, x.size, 8, 0.5, "--hanning_window", outs[0], g.out_floats),
+        (d_in, x.size, 5, 0.5, "--hanning_window", outs[1], g.out_floats),          # exponent below 6
+        (d_in, x.size, 8, 0.5, "--gaussian_window=4<<sigma", outs[2], g.out_floats),  # sigma parse error
+    ])
+    st = ocs_lib.batch_device(reqs)
+    torch.cuda.synchronize()
+    assert st == [0, ocs_lib.OCS_EINVAL, ocs_lib.OCS_EPIPELINE]
+    assert orc.rel_l2(outs[0].cpu().numpy(), orc.fp64_stft(x, 8, 0.5, "--hanning_window")) <= REL_L2
+
+
+def test_batch_cuda_graph_capture(ocs_lib):
+    import torch
+
+    items = _mix(24, seed=4, exps=range(8, 13))
+    bufs = []
+    reqs_in = []
+    for (x, exp, ov, opts) in items:
+        g = ocs_lib.geometry(x.size, exp, ov, opts)
+        d_in = torch.from_numpy(x).cuda()
+        d_out = torch.zeros(g.out_floats, device="cuda")
+        bufs.append((d_in, d_out))
+        reqs_in.append((d_in, x.size, exp, ov, opts, d_out, g.out_floats))
+    reqs = ocs_lib.make_requests(reqs_in)
+    ocs_lib.batch_prepare(reqs)
+    eager = ocs_lib.batch_device(reqs)
+    torch.cuda.synchronize()
+    ref = [b[1].clone() for b in bufs]
+    for b in bufs:
+        b[1].zero_()
+    s = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(graph, stream=s):
+            st = ocs_lib.batch_device(reqs, s)
+    assert st == eager
+    for b in bufs:
+        b[1].zero_()
+    torch.cuda.synchronize()
+    for _ in range(3):
+        graph.replay()
+    torch.cuda.synchronize()
+    for b, r in zip(bufs, ref):
+        assert torch.equal(b[1], r)
