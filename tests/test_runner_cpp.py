@@ -71,7 +71,8 @@ def test_runner_fused_and_stage_paths(built, ocs_lib, orc, exp, ov, opts):
     for mode, got in outs.items():
         assert got.size == ref.size, mode
         assert orc.rel_l2(got, ref) <= 1e-5, mode
-    assert np.array_equal(outs["fused"], ocs_lib.activate(x, exp, ov, opts))
+    # the two processes may autotune to different kernel variants: equal within rounding
+    assert orc.rel_l2(outs["fused"], ocs_lib.activate(x, exp, ov, opts)) <= 1e-6
 
 
 @pytest.mark.gpu
