@@ -128,6 +128,21 @@ int ocs_batch_prepare(const ocs_request* reqs, int count);
  * launch was issued; per-request problems land in reqs[i].status. */
 int ocs_batch_device(ocs_request* reqs, int count, void* stream);
 
+/* Same as ocs_batch_device, for callers that must not allocate GPU memory
+ * (an application that owns the whole device through its own allocator, or
+ * a process that must never block on or fail in cudaMalloc once running).
+ * No counterpart in the reference.  It allocates nothing: its scratch and
+ * tables live in a fixed 1 MiB device array inside the library, held on every
+ * GPU that loads the library until the process exits.  Limits (rejected with
+ * OCS_ENOMEM and a message): at most 256 requests per call, windows 2^6..2^13,
+ * distinct window tables of one call within the array's window region.
+ * Requests with larger windows get status OCS_EINVAL.  The first call on a
+ * device (with that device current) sets the array up and synchronizes
+ * `stream` once; make it before any stream capture.  All calls share the
+ * array: calls whose work overlaps on the GPU race, so order them on one
+ * stream or with events. */
+int ocs_batch_device_noalloc(ocs_request* reqs, int count, void* stream);
+
 /* ---- per-stage hooks: runnerFunction::* (RunnerInterface.hpp:38-76) on
  * device buffers laid out as the reference's [qt][N] planes. ---- */
 

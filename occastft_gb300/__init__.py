@@ -88,6 +88,7 @@ SIGNATURES = {
     "ocs_host_free": (ctypes.c_int, [_VP]),
     "ocs_batch_prepare": (ctypes.c_int, [_VP, ctypes.c_int]),
     "ocs_batch_device": (ctypes.c_int, [_VP, ctypes.c_int, _VP]),
+    "ocs_batch_device_noalloc": (ctypes.c_int, [_VP, ctypes.c_int, _VP]),
     "ocs_stage_overlap": (ctypes.c_int, [_VP, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                          _VP, _VP]),
     "ocs_stage_window": (ctypes.c_int, [ctypes.c_int, _VP, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, _VP]),

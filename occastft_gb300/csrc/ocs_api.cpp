@@ -648,6 +648,10 @@ extern "C" int ocs_batch_device(ocs_request* reqs, int count, void* stream)
     return OCS_OK;
 }
 
+namespace ocs {
+void set_last_error(const std::string& msg) { g_err = msg; }
+}  // namespace ocs
+
 extern "C" {
 
 int ocs_init(int device)

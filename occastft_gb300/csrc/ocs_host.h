@@ -48,4 +48,7 @@ std::string make_geometry(uint64_t n, int exp, float overlap, const Options& o, 
 // cosine, double combine rounded to float.  Empty for WIN_NONE.
 std::vector<float> window_table(int kind, int n_window, float sigma);
 
+// Sets the message ocs_last_error() returns on this thread.
+void set_last_error(const std::string& msg);
+
 }  // namespace ocs
