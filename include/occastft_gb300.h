@@ -143,6 +143,41 @@ int ocs_batch_device(ocs_request* reqs, int count, void* stream);
  * stream or with events. */
 int ocs_batch_device_noalloc(ocs_request* reqs, int count, void* stream);
 
+/* ---- serving: a continuous-batching request server ----
+ * Replaces the reference's one-request-at-a-time WebSocket callback
+ * (GLOBAL/RunnerCommon.cpp:69-134).  Requests (host buffers) queue on submit;
+ * a worker admits them into in-flight slots as slots and device-pool memory
+ * free up, runs each admitted group as one persistent batch launch between
+ * its host->device and device->host copies, and overlaps the slots on the
+ * device.  Latency is submit-to-completion. */
+typedef struct ocs_server_config {
+    uint64_t pool_bytes; /* device pool for in-flight requests; 0 = half of free memory */
+    int max_batch;       /* requests per launch; 0 = 256 */
+    int slots;           /* groups in flight; 0 = 3 */
+} ocs_server_config;
+
+typedef struct ocs_server_stats {
+    uint64_t completed, failed, rejected, pending, batches, samples;
+    double elapsed_ms; /* since start or the last reset */
+    double p50_ms, p99_ms, p999_ms, max_ms;
+    uint64_t pool_bytes, pool_used;
+} ocs_server_stats;
+
+int ocs_server_start(const ocs_server_config* cfg);
+/* Queues one request; in/out are host buffers that must stay valid until
+ * ocs_server_wait returns (pinned buffers copy fastest).  Fails with
+ * OCS_ENOMEM when the request alone exceeds the device pool. */
+int ocs_server_submit(const float* in, uint64_t n, int window_size_exp, float overlap_ratio, const char* options,
+                      float* out, uint64_t out_cap, uint64_t* ticket);
+/* Waits up to timeout_ms (< 0: no limit) for a request; *status is its result. */
+int ocs_server_wait(uint64_t ticket, int timeout_ms, int* status);
+/* Withdraws a request that has not been admitted yet (a client that left). */
+int ocs_server_cancel(uint64_t ticket);
+int ocs_server_get_stats(ocs_server_stats* out);
+int ocs_server_reset_stats(void);
+/* Finishes every queued request, then stops. */
+int ocs_server_stop(void);
+
 /* ---- per-stage hooks: runnerFunction::* (RunnerInterface.hpp:38-76) on
  * device buffers laid out as the reference's [qt][N] planes. ---- */
 

@@ -89,6 +89,14 @@ SIGNATURES = {
     "ocs_batch_prepare": (ctypes.c_int, [_VP, ctypes.c_int]),
     "ocs_batch_device": (ctypes.c_int, [_VP, ctypes.c_int, _VP]),
     "ocs_batch_device_noalloc": (ctypes.c_int, [_VP, ctypes.c_int, _VP]),
+    "ocs_server_start": (ctypes.c_int, [_VP]),
+    "ocs_server_submit": (ctypes.c_int, [_VP, ctypes.c_uint64, ctypes.c_int, ctypes.c_float, ctypes.c_char_p, _VP,
+                                         ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
+    "ocs_server_wait": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    "ocs_server_cancel": (ctypes.c_int, [ctypes.c_uint64]),
+    "ocs_server_get_stats": (ctypes.c_int, [_VP]),
+    "ocs_server_reset_stats": (ctypes.c_int, []),
+    "ocs_server_stop": (ctypes.c_int, []),
     "ocs_stage_overlap": (ctypes.c_int, [_VP, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                          _VP, _VP]),
     "ocs_stage_window": (ctypes.c_int, [ctypes.c_int, _VP, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, _VP]),
@@ -217,6 +225,65 @@ def batch_device(reqs, stream=None) -> list:
     """One persistent launch over all requests; returns the per-request status codes."""
     _check(lib().ocs_batch_device(ctypes.cast(reqs, ctypes.c_void_p), len(reqs), _stream_handle(stream)))
     return [r.status for r in reqs]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("pool_bytes", ctypes.c_uint64), ("max_batch", ctypes.c_int), ("slots", ctypes.c_int)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_uint64) for k in ("completed", "failed", "rejected", "pending", "batches", "samples")] + \
+               [(k, ctypes.c_double) for k in ("elapsed_ms", "p50_ms", "p99_ms", "p999_ms", "max_ms")] + \
+               [("pool_bytes", ctypes.c_uint64), ("pool_used", ctypes.c_uint64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Server:
+    """Continuous-batching request server (host buffers in and out)."""
+
+    def __init__(self, pool_bytes: int = 0, max_batch: int = 0, slots: int = 0):
+        cfg = ServerConfig(pool_bytes, max_batch, slots)
+        _check(lib().ocs_server_start(ctypes.byref(cfg)))
+        self._keep = {}
+
+    def submit(self, x: np.ndarray, window_size_exp: int, overlap_ratio: float, options: str,
+               out: np.ndarray) -> int:
+        t = ctypes.c_uint64()
+        ob = options.encode()
+        _check(lib().ocs_server_submit(x.ctypes.data, x.size, window_size_exp, overlap_ratio, ob,
+                                       out.ctypes.data, out.size, ctypes.byref(t)))
+        self._keep[t.value] = (x, out, ob)
+        return t.value
+
+    def submit_ptr(self, in_ptr: int, n: int, window_size_exp: int, overlap_ratio: float, options: bytes,
+                   out_ptr: int, out_cap: int) -> int:
+        t = ctypes.c_uint64()
+        _check(lib().ocs_server_submit(in_ptr, n, window_size_exp, overlap_ratio, options, out_ptr, out_cap,
+                                       ctypes.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1) -> int:
+        st = ctypes.c_int(-1)
+        _check(lib().ocs_server_wait(ticket, timeout_ms, ctypes.byref(st)))
+        self._keep.pop(ticket, None)
+        return st.value
+
+    def cancel(self, ticket: int) -> None:
+        _check(lib().ocs_server_cancel(ticket))
+        self._keep.pop(ticket, None)
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        _check(lib().ocs_server_get_stats(ctypes.byref(s)))
+        return s.as_dict()
+
+    def reset_stats(self) -> None:
+        _check(lib().ocs_server_reset_stats())
+
+    def stop(self) -> None:
+        _check(lib().ocs_server_stop())
 
 
 class Runner:

@@ -10,6 +10,7 @@
 // compute and device->host copies across frame chunks.
 #include "../../include/occastft_gb300.h"
 #include "ocs_host.h"
+#include "ocs_internal.h"
 #include "ocs_kernels.h"
 
 #include <cuda_runtime.h>
@@ -69,13 +70,9 @@ struct Context {
     std::vector<Slot*> free_slots;
     std::vector<Slot*> all_slots;
     std::map<std::tuple<int, int, int, int>, int> tuned;          // (exp, outk, dense, log2 frames) -> variant
-    // uneven batches: descriptors staged in pinned memory, copied to device scratch
+    // uneven batches: the scratch of ocs_batch_device
     std::mutex batch_mu;
-    char* batch_host = nullptr;
-    size_t batch_host_cap = 0;
-    char* batch_dev = nullptr;
-    size_t batch_dev_cap = 0;
-    cudaEvent_t batch_staged = nullptr;
+    ocs::internal::BatchScratch batch;
     int batch_occ = 0;
     bool tune_loaded = false;
     std::string gpu_name;
@@ -561,45 +558,125 @@ size_t batch_bytes(size_t ndesc, size_t ntiles)
     return align256(ndesc * sizeof(ocs::FusedArgs)) + align256(ntiles * sizeof(ocs::BatchTile)) + 256;
 }
 
-int batch_grow_locked(Context& c, size_t bytes)
+int batch_occ_get()
 {
-    if (c.batch_host_cap < bytes) {
-        if (c.batch_staged) OCS_CUDA(cudaEventSynchronize(c.batch_staged));
-        if (c.batch_host) cudaFreeHost(c.batch_host);
-        c.batch_host = nullptr;
-        c.batch_host_cap = 0;
-        OCS_CUDA(cudaHostAlloc((void**)&c.batch_host, bytes, cudaHostAllocPortable));
-        c.batch_host_cap = bytes;
-    }
-    if (c.batch_dev_cap < bytes) {
-        if (c.batch_dev) {
-            OCS_CUDA(cudaDeviceSynchronize());
-            cudaFree(c.batch_dev);
-        }
-        c.batch_dev = nullptr;
-        c.batch_dev_cap = 0;
-        OCS_CUDA(cudaMalloc((void**)&c.batch_dev, bytes));
-        c.batch_dev_cap = bytes;
-    }
-    if (!c.batch_staged) OCS_CUDA(cudaEventCreateWithFlags(&c.batch_staged, cudaEventDisableTiming));
+    Context& c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
     if (!c.batch_occ) c.batch_occ = std::max(1, ocs::batch_occupancy());
-    return OCS_OK;
+    return c.batch_occ;
 }
 
 }  // namespace
+
+namespace ocs {
+namespace internal {
+
+int batch_scratch_grow(BatchScratch& b, size_t bytes)
+{
+    if (b.host_cap < bytes) {
+        if (b.staged) OCS_CUDA(cudaEventSynchronize(b.staged));
+        if (b.host) cudaFreeHost(b.host);
+        b.host = nullptr;
+        b.host_cap = 0;
+        OCS_CUDA(cudaHostAlloc((void**)&b.host, bytes, cudaHostAllocPortable));
+        b.host_cap = bytes;
+    }
+    if (b.dev_cap < bytes) {
+        if (b.done) OCS_CUDA(cudaEventSynchronize(b.done));
+        if (b.dev) cudaFree(b.dev);
+        b.dev = nullptr;
+        b.dev_cap = 0;
+        OCS_CUDA(cudaMalloc((void**)&b.dev, bytes));
+        b.dev_cap = bytes;
+    }
+    if (!b.staged) OCS_CUDA(cudaEventCreateWithFlags(&b.staged, cudaEventDisableTiming));
+    if (!b.done) OCS_CUDA(cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming));
+    return OCS_OK;
+}
+
+void batch_scratch_release(BatchScratch& b)
+{
+    if (b.host) cudaFreeHost(b.host);
+    if (b.dev) cudaFree(b.dev);
+    if (b.staged) cudaEventDestroy(b.staged);
+    if (b.done) cudaEventDestroy(b.done);
+    b = BatchScratch{};
+}
+
+int batch_prepare_into(const ocs_request* reqs, int count, BatchScratch& b)
+{
+    std::vector<ocs_request> copy(reqs, reqs + count);
+    BatchPlan bp;
+    int rc = batch_build(copy.data(), count, bp, true);
+    if (rc) return rc;
+    batch_occ_get();
+    return batch_scratch_grow(b, batch_bytes(bp.descs.size(), bp.tiles.size()));
+}
+
+// Uploads the descriptors of one batch into `b` and launches the persistent
+// kernel on `st`.  The scratch is reused only after the previous batch that
+// used it has read it (GPU-side wait), so batches on different streams with
+// different scratch objects run concurrently.
+int batch_enqueue(ocs_request* reqs, int count, cudaStream_t st, BatchScratch& b)
+{
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    OCS_CUDA(cudaStreamIsCapturing(st, &cap));
+    const bool capturing = cap != cudaStreamCaptureStatusNone;
+    BatchPlan bp;
+    int rc = batch_build(reqs, count, bp, true);
+    if (rc) return rc;
+    Context& c = ctx();
+    if (!bp.tiles.empty()) {
+        const size_t bytes = batch_bytes(bp.descs.size(), bp.tiles.size());
+        if (capturing && (b.host_cap < bytes || b.dev_cap < bytes))
+            return fail(OCS_ENOMEM, "batch buffers not prepared (call ocs_batch_prepare before capture)");
+        rc = batch_scratch_grow(b, bytes);
+        if (rc) return rc;
+        const int occ = batch_occ_get();
+        if (!capturing) {
+            // the previous batch's descriptors must have left the staging buffer,
+            // and its kernel must be done reading the device copy
+            OCS_CUDA(cudaEventSynchronize(b.staged));
+            OCS_CUDA(cudaStreamWaitEvent(st, b.done, 0));
+        }
+        const size_t o_tiles = align256(bp.descs.size() * sizeof(ocs::FusedArgs));
+        const size_t o_cnt = o_tiles + align256(bp.tiles.size() * sizeof(ocs::BatchTile));
+        std::memcpy(b.host, bp.descs.data(), bp.descs.size() * sizeof(ocs::FusedArgs));
+        std::memcpy(b.host + o_tiles, bp.tiles.data(), bp.tiles.size() * sizeof(ocs::BatchTile));
+        const uint32_t nt = (uint32_t)bp.tiles.size();
+        std::memcpy(b.host + o_cnt, &nt, 4);
+        std::memset(b.host + o_cnt + 4, 0, 4);  // tile counter starts at zero
+        OCS_CUDA(cudaMemcpyAsync(b.dev, b.host, o_cnt + 8, cudaMemcpyHostToDevice, st));
+        if (!capturing) OCS_CUDA(cudaEventRecord(b.staged, st));
+        auto* d_reqs = reinterpret_cast<const ocs::FusedArgs*>(b.dev);
+        auto* d_tiles = reinterpret_cast<const ocs::BatchTile*>(b.dev + o_tiles);
+        auto* d_nt = reinterpret_cast<const uint32_t*>(b.dev + o_cnt);
+        auto* d_cnt = reinterpret_cast<uint32_t*>(b.dev + o_cnt + 4);
+        const int grid = std::max(1, std::min<int>(c.sms * occ, (int)bp.tiles.size()));
+        OCS_CUDA(ocs::launch_batch(d_reqs, d_tiles, d_nt, d_cnt, grid, st));
+        if (!capturing) OCS_CUDA(cudaEventRecord(b.done, st));
+    }
+    for (int i : bp.big) {
+        const Request& r = bp.parsed[i];
+        reqs[i].status = launch_frames(r, reqs[i].in, reqs[i].n, reqs[i].out, 0, r.geo.frames, st);
+    }
+    return OCS_OK;
+}
+
+int ensure_ready() { return ensure_init(); }
+void set_error(int, const std::string& msg) { g_err = msg; }
+
+}  // namespace internal
+}  // namespace ocs
 
 extern "C" int ocs_batch_prepare(const ocs_request* reqs, int count)
 {
     if (count < 0 || (count > 0 && !reqs)) return fail(OCS_EINVAL, "bad request list");
     int rc = ensure_init();
     if (rc) return rc;
-    std::vector<ocs_request> copy(reqs, reqs + count);
-    BatchPlan bp;
-    rc = batch_build(copy.data(), count, bp, true);
-    if (rc) return rc;
     Context& c = ctx();
     std::lock_guard<std::mutex> lk(c.batch_mu);
-    return batch_grow_locked(c, batch_bytes(bp.descs.size(), bp.tiles.size()));
+    return ocs::internal::batch_prepare_into(reqs, count, c.batch);
 }
 
 extern "C" int ocs_batch_device(ocs_request* reqs, int count, void* stream)
@@ -607,45 +684,9 @@ extern "C" int ocs_batch_device(ocs_request* reqs, int count, void* stream)
     if (count < 0 || (count > 0 && !reqs)) return fail(OCS_EINVAL, "bad request list");
     int rc = ensure_init();
     if (rc) return rc;
-    cudaStream_t st = (cudaStream_t)stream;
-    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-    OCS_CUDA(cudaStreamIsCapturing(st, &cap));
-    const bool capturing = cap != cudaStreamCaptureStatusNone;
-    BatchPlan bp;
-    rc = batch_build(reqs, count, bp, true);
-    if (rc) return rc;
     Context& c = ctx();
-    if (!bp.tiles.empty()) {
-        std::lock_guard<std::mutex> lk(c.batch_mu);
-        const size_t bytes = batch_bytes(bp.descs.size(), bp.tiles.size());
-        if (capturing && (c.batch_host_cap < bytes || c.batch_dev_cap < bytes))
-            return fail(OCS_ENOMEM, "batch buffers not prepared (call ocs_batch_prepare before capture)");
-        rc = batch_grow_locked(c, bytes);
-        if (rc) return rc;
-        // the previous batch's descriptors must have left the staging buffer
-        if (!capturing) OCS_CUDA(cudaEventSynchronize(c.batch_staged));
-        const size_t o_tiles = align256(bp.descs.size() * sizeof(ocs::FusedArgs));
-        const size_t o_cnt = o_tiles + align256(bp.tiles.size() * sizeof(ocs::BatchTile));
-        std::memcpy(c.batch_host, bp.descs.data(), bp.descs.size() * sizeof(ocs::FusedArgs));
-        std::memcpy(c.batch_host + o_tiles, bp.tiles.data(), bp.tiles.size() * sizeof(ocs::BatchTile));
-        const uint32_t nt = (uint32_t)bp.tiles.size();
-        std::memcpy(c.batch_host + o_cnt, &nt, 4);
-        std::memset(c.batch_host + o_cnt + 4, 0, 4);  // tile counter starts at zero
-        OCS_CUDA(cudaMemcpyAsync(c.batch_dev, c.batch_host, o_cnt + 8, cudaMemcpyHostToDevice, st));
-        if (!capturing) OCS_CUDA(cudaEventRecord(c.batch_staged, st));
-        auto* d_reqs = reinterpret_cast<const ocs::FusedArgs*>(c.batch_dev);
-        auto* d_tiles = reinterpret_cast<const ocs::BatchTile*>(c.batch_dev + o_tiles);
-        auto* d_nt = reinterpret_cast<const uint32_t*>(c.batch_dev + o_cnt);
-        auto* d_cnt = reinterpret_cast<uint32_t*>(c.batch_dev + o_cnt + 4);
-        const int grid = std::max(1, std::min<int>(c.sms * c.batch_occ, (int)bp.tiles.size()));
-        OCS_CUDA(ocs::launch_batch(d_reqs, d_tiles, d_nt, d_cnt, grid, st));
-    }
-    for (int i : bp.big) {
-        const Request& r = bp.parsed[i];
-        rc = launch_frames(r, reqs[i].in, reqs[i].n, reqs[i].out, 0, r.geo.frames, st);
-        reqs[i].status = rc;
-    }
-    return OCS_OK;
+    std::lock_guard<std::mutex> lk(c.batch_mu);
+    return ocs::internal::batch_enqueue(reqs, count, (cudaStream_t)stream, c.batch);
 }
 
 namespace ocs {
@@ -685,13 +726,7 @@ void ocs_shutdown(void)
     c.all_slots.clear();
     c.free_slots.clear();
     c.occupancy.clear();
-    if (c.batch_host) cudaFreeHost(c.batch_host);
-    if (c.batch_dev) cudaFree(c.batch_dev);
-    if (c.batch_staged) cudaEventDestroy(c.batch_staged);
-    c.batch_host = nullptr;
-    c.batch_dev = nullptr;
-    c.batch_staged = nullptr;
-    c.batch_host_cap = c.batch_dev_cap = 0;
+    ocs::internal::batch_scratch_release(c.batch);
     c.batch_occ = 0;
     if (c.s_setup) cudaStreamDestroy(c.s_setup);
     c.s_setup = nullptr;
