@@ -342,6 +342,135 @@ def run_batch_leg(ocs, steps: int, warmup: int, count: int = 4096):
     return res
 
 
+def pinned(ocs, nfloats: int):
+    import ctypes
+
+    p = ctypes.c_void_p()
+    ocs._check(ocs.lib().ocs_host_alloc(ctypes.byref(p), nfloats * 4))
+    return p.value, np.ctypeslib.as_array((ctypes.c_float * nfloats).from_address(p.value))
+
+
+def link_bandwidth(ocs):
+    """Host<->device copy bandwidth with pinned buffers (the bound of served traffic)."""
+    import torch
+
+    n = 1 << 27  # 512 MB
+    hp, hx = pinned(ocs, n)
+    hx[:] = 1.0
+    d = torch.empty(n, device="cuda")
+    h = torch.from_numpy(hx)
+    for _ in range(2):
+        d.copy_(h, non_blocking=True)
+        h.copy_(d, non_blocking=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(4):
+        d.copy_(h, non_blocking=True)
+    torch.cuda.synchronize()
+    h2d = 4 * n * 4 / (time.perf_counter() - t0) / 1e9
+    t0 = time.perf_counter()
+    for _ in range(4):
+        h.copy_(d, non_blocking=True)
+    torch.cuda.synchronize()
+    d2h = 4 * n * 4 / (time.perf_counter() - t0) / 1e9
+    del d, h
+    ocs.lib().ocs_host_free(hp)
+    return {"h2d_gbs": round(h2d, 1), "d2h_gbs": round(d2h, 1)}
+
+
+def draw_served(rng, count):
+    """Request draws: length log-uniform [2^14, 2^24], window/overlap/type as in the uneven batch,
+    half power, half half-complex."""
+    lens = np.round(2.0 ** rng.uniform(14, 24, count)).astype(np.int64)
+    exps = rng.choice([8, 9, 10, 11, 12], count)
+    ovs = rng.choice([0.25, 0.5, 0.75], count)
+    wins = rng.choice(["--hanning_window", "--hamming_window", "--blackman_window"], count)
+    half = rng.random(count) < 0.5
+    opts = [(w + (" --half_complex_return" if h else "")).encode() for w, h in zip(wins, half)]
+    return lens, exps, ovs, opts
+
+
+def run_serving_leg(ocs, rates=(2000, 10000, 50000), durations=(1.0, 0.5, 0.3), seed=3):
+    """Poisson request stream against the continuous-batching server (host buffers in and out),
+    and the same draws served one at a time through ocs_activate."""
+    import ctypes
+
+    import torch
+
+    res = {"link": link_bandwidth(ocs)}
+    pool_n = 1 << 26
+    ip, ix = pinned(ocs, pool_n)  # signal pool: noise + chirp, requests read slices of it
+    g = np.random.default_rng(seed)
+    ix[:] = g.uniform(-1, 1, pool_n).astype(np.float32)
+    t = np.arange(pool_n, dtype=np.float64) / FS
+    ix[:] += np.sin(2 * np.pi * (100.0 * t + 9900.0 * t * t / (2 * t[-1]))).astype(np.float32)
+    out_n = 1 << 28
+    op, _ = pinned(ocs, out_n)
+    max_out = 1 << 26 + 1
+    srv = ocs.Server(pool_bytes=48 << 30, max_batch=256, slots=4)
+    rows = []
+    try:
+        for rate, dur in zip(rates, durations):
+            rng = np.random.default_rng(seed + rate)
+            count = int(rate * dur)
+            arrivals = np.cumsum(rng.exponential(1.0 / rate, count))
+            lens, exps, ovs, opts = draw_served(rng, count)
+            starts = rng.integers(0, pool_n - lens.max(), count)
+            geos = [ocs.geometry(int(lens[i]), int(exps[i]), float(ovs[i]), opts[i].decode()) for i in range(count)]
+            ooff = 0
+            srv.reset_stats()
+            tickets = []
+            t0 = time.perf_counter()
+            for i in range(count):
+                while time.perf_counter() - t0 < arrivals[i]:
+                    pass
+                of = geos[i].out_floats
+                if ooff + of > out_n:
+                    ooff = 0
+                tickets.append(srv.submit_ptr(ip + 4 * int(starts[i]), int(lens[i]), int(exps[i]), float(ovs[i]),
+                                              opts[i], op + 4 * ooff, of))
+                ooff += (of + 63) // 64 * 64
+            for tk in tickets:
+                srv.wait(tk, 600000)
+            wall = time.perf_counter() - t0
+            st = srv.stats()
+            rows.append({"offered_req_s": rate, "requests": count, "wall_s": round(wall, 3),
+                         "achieved_req_s": round(count / wall, 1),
+                         "gsamples_s": round(int(lens.sum()) / wall / 1e9, 2),
+                         "p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
+                         "p999_ms": round(st["p999_ms"], 3), "batches": st["batches"],
+                         "mean_batch": round(count / max(1, st["batches"]), 1)})
+        # plain: the same kind of draws, one synchronous ocs_activate per request
+        rng = np.random.default_rng(seed + 1)
+        lens, exps, ovs, opts = draw_served(rng, 400)
+        starts = rng.integers(0, pool_n - lens.max(), 400)
+        L = ocs.lib()
+        nlen = ctypes.c_uint64()
+        done = 0
+        t0 = time.perf_counter()
+        for i in range(400):
+            of = ocs.geometry(int(lens[i]), int(exps[i]), float(ovs[i]), opts[i].decode()).out_floats
+            ocs._check(L.ocs_activate(ip + 4 * int(starts[i]), int(lens[i]), int(exps[i]), float(ovs[i]), opts[i],
+                                      op, of, ctypes.byref(nlen)))
+            done += int(lens[i])
+            if time.perf_counter() - t0 > 3.0:
+                break
+        plain = done / (time.perf_counter() - t0) / 1e9
+    finally:
+        srv.stop()
+        ocs.lib().ocs_host_free(ip)
+        ocs.lib().ocs_host_free(op)
+    res["rates"] = rows
+    res["plain_per_request_gsamples_s"] = round(plain, 2)
+    best = max(r["gsamples_s"] for r in rows)
+    res["served_vs_plain"] = round(best / plain, 2)
+    res["workload"] = ("Poisson arrivals; length log-uniform [2^14, 2^24], window {256..4096}, overlap "
+                       "{0.25,0.5,0.75}, Hann/Hamming/Blackman, half power / half half-complex; pinned host "
+                       "buffers; latency = submit to result in host memory")
+    torch.cuda.empty_cache()
+    return res
+
+
 def run_ours(args):
     import torch
 
@@ -496,6 +625,9 @@ def run_ours(args):
     batch = None
     if rank == 0 and not args.no_batch:
         batch = run_batch_leg(ocs, steps=5, warmup=3)
+    serving = None
+    if rank == 0 and not args.no_serve:
+        serving = run_serving_leg(ocs)
 
     if rank != 0:
         if ws > 1:
@@ -527,6 +659,7 @@ def run_ours(args):
         "sweep": sweep,
         "cufft_reference": cufft,
         "uneven_batch": batch,
+        "serving": serving,
     }
     print(json.dumps(line))
     if ws > 1:
@@ -546,6 +679,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--n", type=int, default=N_SAMPLES, help="signal samples (profiling runs use fewer)")
     ap.add_argument("--exp", type=int, default=HEAD_EXP)
     ap.add_argument("--options", default=HEAD_OPTS)
