@@ -21,7 +21,7 @@ RUNNER_LIB = os.path.join(PKG, "libocs_runner.so")
 RUNNER_DEMO = os.path.join(PKG, "ocs_runner_demo")
 
 CU_SOURCES = ["stft_fused.cu", "stft_fused_lo.cu", "stft_fused_hi.cu", "stft_pair_lo.cu", "stft_pair_hi.cu",
-              "stft_batch.cu", "stft_batch_noalloc.cu", "stft_stages.cu"]
+              "stft_batch.cu", "stft_batch_noalloc.cu", "stft_tc.cu", "stft_stages.cu"]
 CPP_SOURCES = ["ocs_api.cpp", "ocs_host.cpp", "ocs_server.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

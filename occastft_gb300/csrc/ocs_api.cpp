@@ -74,6 +74,7 @@ struct Context {
     std::mutex batch_mu;
     ocs::internal::BatchScratch batch;
     int batch_occ = 0;
+    int* d_err = nullptr;  // device error word of the bounded waits in the tensor-core kernel
     bool tune_loaded = false;
     std::string gpu_name;
 };
@@ -100,6 +101,8 @@ int init_locked(Context& c, int device)
     c.sms = p.multiProcessorCount;
     c.gpu_name = p.name;
     OCS_CUDA(cudaStreamCreateWithFlags(&c.s_setup, cudaStreamNonBlocking));
+    OCS_CUDA(cudaMalloc(&c.d_err, sizeof(int)));
+    OCS_CUDA(cudaMemset(c.d_err, 0, sizeof(int)));
     c.ready = true;
     return OCS_OK;
 }
@@ -260,6 +263,8 @@ int prepare(uint64_t n, int exp, float ov, const char* options, Request& r)
     if (st != "OK") return fail(OCS_EPIPELINE, st);
     st = ocs::make_geometry(n, exp, ov, r.opt, r.geo);
     if (st != "OK") return fail(OCS_EINVAL, st);
+    if (r.opt.precision == 1 && !ocs::tc_supports(exp))
+        return fail(OCS_EINVAL, "the tensor-core form supports windows 2^8 and 2^10");
     r.exp = exp;
     return OCS_OK;
 }
@@ -336,6 +341,17 @@ int launch_frames(const Request& r, const float* d_sig, uint64_t n, float* d_out
     a.vec2 = (hop % 2 == 0) && ((xa & 7u) == 0);
     a.cs = ((hop % 4 == 0) && (xa & 15u) == 0) ? 16 : (a.vec2 ? 8 : 4);
     const bool out16 = (reinterpret_cast<uintptr_t>(a.out) & 15u) == 0;
+
+    if (r.opt.precision == 1) {
+        // tensor-core form: unscaled window (no real-input untangle)
+        const float* w1 = nullptr;
+        rc = get_window(r.opt.window, r.exp, r.opt.sigma, false, &w1);
+        if (rc) return rc;
+        a.win = w1;
+        Context& c = ctx();
+        OCS_CUDA(ocs::launch_tc(r.exp, outk, a, c.d_err, c.sms, st));
+        return OCS_OK;
+    }
 
     int cand[3], nc = 0;
     for (int v = 0; v < 3; ++v)
@@ -728,6 +744,8 @@ void ocs_shutdown(void)
     c.occupancy.clear();
     ocs::internal::batch_scratch_release(c.batch);
     c.batch_occ = 0;
+    if (c.d_err) cudaFree(c.d_err);
+    c.d_err = nullptr;
     if (c.s_setup) cudaStreamDestroy(c.s_setup);
     c.s_setup = nullptr;
     c.ready = false;

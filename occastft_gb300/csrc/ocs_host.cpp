@@ -51,6 +51,7 @@ std::string parse_options(const char* options, Options& o)
     o.half_complex = s.find("--half_complex_return") != std::string::npos;
     o.dense = s.find("--layout=dense") != std::string::npos;
     o.serial_power = s.find("--serial_power") != std::string::npos;
+    if (s.find("--precision=tc-fp16") != std::string::npos) o.precision = 1;
     return "OK";
 }
 

@@ -26,6 +26,7 @@ struct Options {
     bool half_complex = false;
     bool dense = false;
     bool serial_power = false;
+    int precision = 0;  // 0 plain FP32; 1 tensor cores, fp16 hi/lo split (--precision=tc-fp16)
 };
 
 struct Geometry {

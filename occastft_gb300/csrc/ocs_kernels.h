@@ -63,6 +63,10 @@ size_t batch_smem_bytes();
 cudaError_t launch_batch(const FusedArgs* d_reqs, const BatchTile* d_tiles, const uint32_t* d_ntiles,
                          uint32_t* d_counter, int grid, cudaStream_t st);
 
+// tensor-core split-precision form (tcgen05), windows 2^8 and 2^10
+bool tc_supports(int exp);
+cudaError_t launch_tc(int exp, int outk, const FusedArgs& a, int* err, int sms, cudaStream_t st);
+
 // unfused per-stage kernels behind the runnerFunction hooks
 cudaError_t launch_overlap(const float* in, uint32_t ofull, uint32_t n, uint32_t exp, uint32_t hop,
                            float* real, cudaStream_t st);
