@@ -471,6 +471,45 @@ def run_serving_leg(ocs, rates=(2000, 10000, 50000), durations=(1.0, 0.5, 0.3), 
     return res
 
 
+def run_tc_leg(ocs, x, n, d_out, stream, steps=10, warmup=3):
+    """Windows 256..4096, Hann, overlap 0.75 on the 1e8-sample signal: plain FP32
+    against the tensor-core split-precision form, with accuracy vs FP64."""
+    import torch
+
+    from oracle import orc
+
+    peak, _ = load_peaks()
+    rows = []
+    # overlap 0.75 writes ~4 floats per input sample
+    d_out = torch.empty(max(ocs.geometry(n, e, 0.75, "").out_floats for e in (8, 9, 10, 11, 12)), device="cuda")
+    for exp in (8, 9, 10, 11, 12):
+        for prec in ("fp32", "tc-fp16"):
+            opts = "--hanning_window" + (" --precision=tc-fp16" if prec != "fp32" else "")
+            try:
+                g = ocs.geometry(n, exp, 0.75, opts)
+            except ocs.OcsError:
+                continue
+            if g.out_floats > d_out.numel():
+                continue
+            dt = time_device(ocs, x, n, exp, 0.75, opts, d_out, d_out.numel(), steps, warmup, stream)
+            # accuracy on 300 frames from the middle of the signal
+            nf = 300
+            f0 = g.qt // 2
+            s0 = f0 * g.hop
+            xs = x[s0:s0 + (nf - 1) * g.hop + g.n_window].cpu().numpy()
+            got = d_out[f0 * g.n_window:(f0 + nf) * g.n_window].cpu().numpy()
+            ref = orc.fp64_stft(xs, exp, 0.75, "--hanning_window")[: nf * g.n_window]
+            b = algorithmic_bytes(n, g, False, False)
+            rows.append({"N": 1 << exp, "precision": prec, "gsamples_s": round(n / dt / 1e9, 2),
+                         "ms": round(dt * 1e3, 4), "hbm_frac": round(b / dt / 1e9 / peak, 3),
+                         "rel_l2_vs_fp64": float("%.3g" % orc.rel_l2(got, ref)),
+                         "max_db_vs_fp64": round(orc.max_db_error(got, ref), 4)})
+    del d_out
+    torch.cuda.empty_cache()
+    return {"rows": rows, "workload": "1e8-sample multi-sinusoid signal, Hann, overlap 0.75, power (reference "
+                                      "layout); tc-fp16 = tcgen05 four-step FFT with fp16 hi/lo products"}
+
+
 def run_ours(args):
     import torch
 
@@ -622,6 +661,9 @@ def run_ours(args):
                          "unfold*window->rfft->abs pipeline (N/2+1 bins), same GPU"}
         del frames
 
+    tc = None
+    if rank == 0 and not args.no_sweep:
+        tc = run_tc_leg(ocs, x, n, d_out, stream)
     batch = None
     if rank == 0 and not args.no_batch:
         batch = run_batch_leg(ocs, steps=5, warmup=3)
@@ -658,6 +700,7 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "sweep": sweep,
         "cufft_reference": cufft,
+        "tensor_core": tc,
         "uneven_batch": batch,
         "serving": serving,
     }
@@ -683,10 +726,11 @@ def main():
     ap.add_argument("--n", type=int, default=N_SAMPLES, help="signal samples (profiling runs use fewer)")
     ap.add_argument("--exp", type=int, default=HEAD_EXP)
     ap.add_argument("--options", default=HEAD_OPTS)
+    ap.add_argument("--overlap", type=float, default=HEAD_OV)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    globals().update(N_SAMPLES=args.n, HEAD_EXP=args.exp, HEAD_OPTS=args.options)
+    globals().update(N_SAMPLES=args.n, HEAD_EXP=args.exp, HEAD_OPTS=args.options, HEAD_OV=args.overlap)
     if args.impl == "reference":
         run_reference_arm(args)
     else:

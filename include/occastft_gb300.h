@@ -84,7 +84,10 @@ int ocs_activate(const float* in, uint64_t n, int window_size_exp, float overlap
 
 /* The device half of ActivateSTFT: runnerFunction::Default_Pipeline
  * (RunnerCommon.cpp:184-316) on device-resident buffers, fused into one
- * kernel launch on `stream`, asynchronous. */
+ * kernel launch on `stream`, asynchronous.  With --precision=tc-fp16 a wait
+ * inside the tensor-core kernel that gives up (after about a second) is
+ * reported as OCS_ETIMEDOUT by ocs_activate at once and, since this call
+ * does not synchronise, by the next tensor-core call of this function. */
 int ocs_activate_device(const float* d_in, uint64_t n, int window_size_exp, float overlap_ratio,
                         const char* options, float* d_out, uint64_t out_cap, void* stream);
 

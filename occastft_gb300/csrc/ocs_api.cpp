@@ -74,7 +74,11 @@ struct Context {
     std::mutex batch_mu;
     ocs::internal::BatchScratch batch;
     int batch_occ = 0;
-    int* d_err = nullptr;  // device error word of the bounded waits in the tensor-core kernel
+    // error word of the bounded waits in the tensor-core kernels: mapped host
+    // memory, so the host reads it without a copy or a stream order
+    int* h_err = nullptr;
+    int* d_err = nullptr;
+    int tc_test_stall = 0;  // OCS_TC_TEST_STALL=1: the kernel's first input phase never completes
     bool tune_loaded = false;
     std::string gpu_name;
 };
@@ -101,10 +105,26 @@ int init_locked(Context& c, int device)
     c.sms = p.multiProcessorCount;
     c.gpu_name = p.name;
     OCS_CUDA(cudaStreamCreateWithFlags(&c.s_setup, cudaStreamNonBlocking));
-    OCS_CUDA(cudaMalloc(&c.d_err, sizeof(int)));
-    OCS_CUDA(cudaMemset(c.d_err, 0, sizeof(int)));
+    OCS_CUDA(cudaHostAlloc(&c.h_err, sizeof(int), cudaHostAllocMapped));
+    *reinterpret_cast<volatile int*>(c.h_err) = 0;
+    OCS_CUDA(cudaHostGetDevicePointer(&c.d_err, c.h_err, 0));
+    const char* stall = std::getenv("OCS_TC_TEST_STALL");
+    c.tc_test_stall = (stall && stall[0] == '1') ? 1 : 0;
     c.ready = true;
     return OCS_OK;
+}
+
+// Reads and clears the tensor-core error word.  The kernels write it
+// directly into mapped host memory, so once their stream has been
+// synchronised the value is current.
+int take_tc_error()
+{
+    Context& c = ctx();
+    if (!c.h_err) return OCS_OK;
+    volatile int* w = reinterpret_cast<volatile int*>(c.h_err);
+    if (*w == 0) return OCS_OK;
+    *w = 0;
+    return fail(OCS_ETIMEDOUT, "tensor-core kernel: a pipeline wait gave up after one second");
 }
 
 int ensure_init()
@@ -349,7 +369,7 @@ int launch_frames(const Request& r, const float* d_sig, uint64_t n, float* d_out
         if (rc) return rc;
         a.win = w1;
         Context& c = ctx();
-        OCS_CUDA(ocs::launch_tc(r.exp, outk, a, c.d_err, c.sms, st));
+        OCS_CUDA(ocs::launch_tc(r.exp, outk, a, c.d_err, c.tc_test_stall, c.sms, st));
         return OCS_OK;
     }
 
@@ -744,7 +764,8 @@ void ocs_shutdown(void)
     c.occupancy.clear();
     ocs::internal::batch_scratch_release(c.batch);
     c.batch_occ = 0;
-    if (c.d_err) cudaFree(c.d_err);
+    if (c.h_err) cudaFreeHost(c.h_err);
+    c.h_err = nullptr;
     c.d_err = nullptr;
     if (c.s_setup) cudaStreamDestroy(c.s_setup);
     c.s_setup = nullptr;
@@ -781,6 +802,11 @@ int ocs_activate_device(const float* d_in, uint64_t n, int exp, float ov, const 
     if (!d_in || !d_out) return fail(OCS_EINVAL, "null buffer");
     rc = ensure_init();
     if (rc) return rc;
+    // asynchronous: a timed-out earlier tensor-core launch is reported here
+    if (r.opt.precision == 1) {
+        rc = take_tc_error();
+        if (rc) return rc;
+    }
     return launch_frames(r, d_in, n, d_out, 0, r.geo.frames, (cudaStream_t)stream);
 }
 
@@ -839,6 +865,10 @@ int ocs_activate(const float* in, uint64_t n, int exp, float ov, const char* opt
     if (e != cudaSuccess) return cuda_fail(e, "ocs_activate");
     if (e2 != cudaSuccess) return cuda_fail(e2, "ocs_activate sync");
     if (e3 != cudaSuccess) return cuda_fail(e3, "ocs_activate sync");
+    if (r.opt.precision == 1) {
+        rc = take_tc_error();
+        if (rc) return rc;
+    }
     if (out_len) *out_len = r.geo.out_floats;
     return OCS_OK;
 }

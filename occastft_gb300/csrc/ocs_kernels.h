@@ -65,7 +65,10 @@ cudaError_t launch_batch(const FusedArgs* d_reqs, const BatchTile* d_tiles, cons
 
 // tensor-core split-precision form (tcgen05), windows 2^8 and 2^10
 bool tc_supports(int exp);
-cudaError_t launch_tc(int exp, int outk, const FusedArgs& a, int* err, int sms, cudaStream_t st);
+// err: word the kernel sets to 1 when a pipeline wait gives up (after about a
+// second); test_stall: test hook, the first input phase of each CTA never
+// completes so that every wait runs out
+cudaError_t launch_tc(int exp, int outk, const FusedArgs& a, int* err, int test_stall, int sms, cudaStream_t st);
 
 // unfused per-stage kernels behind the runnerFunction hooks
 cudaError_t launch_overlap(const float* in, uint32_t ofull, uint32_t n, uint32_t exp, uint32_t hop,

@@ -26,6 +26,7 @@
 #include <cuda_fp16.h>
 
 #include <cstdint>
+#include <mutex>
 
 namespace ocs {
 namespace {
@@ -437,7 +438,596 @@ __global__ void __launch_bounds__(128, 1) stft_tc_kernel(const FusedArgs a, int*
     if (warp == 0) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(C::TMEM_COLS));
     }
-    if (aborted && tid == 0) atomicExch(err, 1);
+    if (aborted && tid == 0) *reinterpret_cast<volatile int*>(err) = 1;
+}
+
+
+// ============================================================ pipelined form
+// Warp roles (448 threads, 14 warps):
+//   warps 0-3   loaders: window, DC, per-frame scale, fp16 split -> A1[s]
+//   warps 4-7   epilogue 1: D1 -> twiddle -> split -> A2[s]
+//   warps 8-11  epilogue 2: D2 -> power / half-complex -> global memory
+//   warp 12     one thread issues every MMA (both passes)
+//   warp 13     one thread prefetches each tile's input span (TMA bulk copy)
+// Operands (A1, A2), accumulators (D1, D2 in tensor memory) and the raw input
+// are double-buffered, so the four stages work on different tiles at once.
+// The DFT matrices and twiddles are built once per window size into global
+// memory, already in the swizzled shared-memory image, and copied per CTA.
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(b)), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(b)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* b)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(b))
+                 : "memory");
+}
+
+// Waits for the phase of the given parity.  Gives up after one second of
+// wall time (globaltimer) or as soon as another role of the CTA has given up.
+__device__ __forceinline__ bool mbar_wait_t(uint64_t* mbar, uint32_t parity, const volatile int* abort_flag)
+{
+    const uint32_t a = smem_u32(mbar);
+    uint64_t t0 = 0;
+    for (uint32_t i = 0; i < (1u << 30); ++i) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(ok)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if ((i & 63) == 63) {
+            if (abort_flag && *abort_flag) return false;
+            uint64_t t;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+            if (t0 == 0) t0 = t;
+            else if (t - t0 > 1000000000ull) return false;
+        }
+    }
+    return false;
+}
+
+// fp16 hi/lo split with packed conversions (two values per instruction)
+__device__ __forceinline__ void split8p(const float (&x)[8], uint4& hi, uint4& lo)
+{
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const __half2 a = __floats2half2_rn(x[2 * i], x[2 * i + 1]);
+        const float2 b = __half22float2(a);
+        const __half2 c = __floats2half2_rn(x[2 * i] - b.x, x[2 * i + 1] - b.y);
+        h[i] = *reinterpret_cast<const uint32_t*>(&a);
+        l[i] = *reinterpret_cast<const uint32_t*>(&c);
+    }
+    hi = make_uint4(h[0], h[1], h[2], h[3]);
+    lo = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+template <int R>
+struct Tc2Cfg {
+    static constexpr int N = R * R;
+    static constexpr int FPT = 128 / R;
+    static constexpr int K1 = R, K2 = 2 * R, NO = 2 * R;
+    static constexpr uint32_t RAW_BYTES = ((FPT * N + 64) * 4 + 1023) / 1024 * 1024;  // span of hop <= N
+    static constexpr uint32_t A1_BYTES = 2 * (K1 / 8) * 2048;
+    static constexpr uint32_t A2_BYTES = 2 * (K2 / 8) * 2048;
+    static constexpr uint32_t B1_BYTES = 2 * NO * 128;
+    static constexpr uint32_t B2_BYTES = 2 * NO * 128;
+    static constexpr uint32_t TW_BYTES = N * 8;
+    static constexpr uint32_t TAB_BYTES = B1_BYTES + B2_BYTES + TW_BYTES;  // the prebuilt image
+    static constexpr uint32_t OFF_RAW = 0;
+    static constexpr uint32_t OFF_A1 = OFF_RAW + 2 * RAW_BYTES;
+    static constexpr uint32_t OFF_A2 = OFF_A1 + 2 * A1_BYTES;
+    static constexpr uint32_t OFF_B1 = OFF_A2 + 2 * A2_BYTES;
+    static constexpr uint32_t OFF_B2 = OFF_B1 + B1_BYTES;
+    static constexpr uint32_t OFF_TW = OFF_B2 + B2_BYTES;
+    static constexpr uint32_t OFF_WIN = OFF_TW + TW_BYTES;
+    static constexpr uint32_t OFF_BAR = OFF_WIN + N * 4;
+    static constexpr uint32_t OFF_MISC = OFF_BAR + 32 * 8;
+    static constexpr uint32_t SMEM = OFF_MISC + 512 + 1024;
+    static constexpr uint32_t TMEM_COLS = 4 * NO <= 128 ? 128 : 256;
+    static_assert(TAB_BYTES % 16 == 0, "table image copied in 16-byte units");
+};
+
+__device__ __align__(1024) unsigned char g_tc_tab16[Tc2Cfg<16>::TAB_BYTES];
+__device__ __align__(1024) unsigned char g_tc_tab32[Tc2Cfg<32>::TAB_BYTES];
+
+// B1: rows 2k1 (re), 2k1+1 (im) of the real-input r-point DFT, K = m.
+// B2: the complex r-point DFT as a real matrix, K = g (re part, k < R) and
+// g (im part, k >= R).  TW: W_N^{g k1} / R, stored [k1][g].
+template <int R>
+__global__ void build_tc_tables_kernel(unsigned char* img)
+{
+    using C = Tc2Cfg<R>;
+    unsigned char* B1 = img;
+    unsigned char* B2 = img + C::B1_BYTES;
+    float2* TW = reinterpret_cast<float2*>(img + C::B1_BYTES + C::B2_BYTES);
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    for (int e = tid; e < C::NO * C::K1; e += nth) {
+        const int row = e / C::K1, m = e % C::K1, k1 = row >> 1;
+        double sn, cs;
+        sincospi(2.0 * (double)((m * k1) % R) / (double)R, &sn, &cs);
+        const float w = (row & 1) ? (float)(-sn) : (float)cs;
+        const __half h = __float2half_rn(w), l = __float2half_rn(w - __half2float(h));
+        *reinterpret_cast<__half*>(B1 + k_off(row, m)) = h;
+        *reinterpret_cast<__half*>(B1 + C::B1_BYTES / 2 + k_off(row, m)) = l;
+    }
+    for (int e = tid; e < C::NO * C::K2; e += nth) {
+        const int row = e / C::K2, k = e % C::K2, k2 = row >> 1, g = k % R;
+        double sn, cs;
+        sincospi(2.0 * (double)((g * k2) % R) / (double)R, &sn, &cs);
+        // (yr + i yi)(c - i s): re = yr c + yi s, im = yi c - yr s
+        float w;
+        if ((row & 1) == 0) w = (k < R) ? (float)cs : (float)sn;
+        else w = (k < R) ? (float)(-sn) : (float)cs;
+        const __half h = __float2half_rn(w), l = __float2half_rn(w - __half2float(h));
+        *reinterpret_cast<__half*>(B2 + k_off(row, k)) = h;
+        *reinterpret_cast<__half*>(B2 + C::B2_BYTES / 2 + k_off(row, k)) = l;
+    }
+    for (int e = tid; e < C::N; e += nth) {
+        const int k1 = e / R, g = e % R;
+        double sn, cs;
+        sincospi(2.0 * (double)((g * k1) % C::N) / (double)C::N, &sn, &cs);
+        // 1/R is a power of two: folding it in changes no rounding
+        TW[e] = make_float2((float)cs / (float)R, (float)(-sn) / (float)R);
+    }
+}
+
+enum { B_RAW_FULL = 0, B_RAW_EMPTY = 2, B_A1_FULL = 4, B_A1_EMPTY = 6, B_D1_FULL = 8, B_D1_EMPTY = 10,
+       B_A2_FULL = 12, B_A2_EMPTY = 14, B_D2_FULL = 16, B_D2_EMPTY = 18, B_FIN = 20, B_COUNT = 21 };
+
+constexpr int kTc2Threads = 448;
+
+template <int R, int OUTK>
+__global__ void __launch_bounds__(kTc2Threads, 1)
+    stft_tc2_kernel(const FusedArgs a, const unsigned char* __restrict__ tab, volatile int* err, int test_stall)
+{
+    using C = Tc2Cfg<R>;
+    constexpr int N = C::N, FPT = C::FPT;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* sm = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    float* RAW = reinterpret_cast<float*>(sm + C::OFF_RAW);
+    unsigned char* A1 = sm + C::OFF_A1;
+    unsigned char* A2 = sm + C::OFF_A2;
+    const float2* TW = reinterpret_cast<const float2*>(sm + C::OFF_TW);
+    float* WIN = reinterpret_cast<float*>(sm + C::OFF_WIN);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + C::OFF_BAR);
+    unsigned char* misc = sm + C::OFF_MISC;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(misc);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(misc + 8);
+    uint64_t* raw_base = reinterpret_cast<uint64_t*>(misc + 16);  // [2]
+    uint64_t* raw_end = reinterpret_cast<uint64_t*>(misc + 32);   // [2]
+    // per-frame scales travel with the tile: loaders -> sA -> (MMA thread) sB
+    // -> (epilogue 1) sC -> (MMA thread) sD -> epilogue 2; each copy happens
+    // between the wait on a stage's "full" barrier and the release of its
+    // "empty" one, so no slot is rewritten while still being read
+    float* sA = reinterpret_cast<float*>(misc + 64);
+    float* sB = sA + 2 * FPT;
+    float* sC = sB + 2 * FPT;
+    float* sD = sC + 2 * FPT;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    if (tid == 0) {
+        for (int s = 0; s < 2; ++s) {
+            mbar_init(&bar[B_RAW_FULL + s], 1);
+            mbar_init(&bar[B_RAW_EMPTY + s], 128);
+            mbar_init(&bar[B_A1_FULL + s], 128);
+            mbar_init(&bar[B_A1_EMPTY + s], 1);
+            mbar_init(&bar[B_D1_FULL + s], 2);  // MMA completion + the thread's copy of the scales
+            mbar_init(&bar[B_D1_EMPTY + s], 128);
+            mbar_init(&bar[B_A2_FULL + s], 128);
+            mbar_init(&bar[B_A2_EMPTY + s], 1);
+            mbar_init(&bar[B_D2_FULL + s], 2);
+            mbar_init(&bar[B_D2_EMPTY + s], 128);
+        }
+        mbar_init(&bar[B_FIN], 1);
+        *abort_flag = 0;
+    }
+    if (warp == 12) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                     "r"(C::TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(tab);
+        uint4* dst = reinterpret_cast<uint4*>(sm + C::OFF_B1);
+        for (int e = tid; e < (int)(C::TAB_BYTES / 16); e += kTc2Threads) dst[e] = src[e];
+        // window stored so that the float4 a lane needs for (j, h) sits at
+        // WIN[((2 j + h) * 32 + lane) * 4]: one warp-wide load reads 512
+        // contiguous bytes (lane owns samples 8 (lane + 32 j) .. + 7)
+        for (int e = tid; e < N; e += kTc2Threads) {
+            const int c = e >> 3, h = (e >> 2) & 1, k = e & 3, ln = c & 31, j = c >> 5;
+            WIN[((2 * j + h) * 32 + ln) * 4 + k] = a.win ? a.win[e] : 1.0f;
+        }
+    }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tmem_slot;
+    constexpr uint32_t ID = idesc_f16(128, C::NO);
+
+    const uint64_t ntiles = (a.frames + FPT - 1) / FPT;
+    const uint64_t cnt = blockIdx.x < ntiles ? (ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+    auto tile_of = [&](uint64_t i) { return blockIdx.x + i * gridDim.x; };
+    auto give_up = [&]() {
+        *abort_flag = 1;
+        *err = 1;
+    };
+    // Samples are addressed from xb = a.x rounded down to 16 bytes (the same
+    // 16-byte block, so still inside the caller's allocation): sample gi sits
+    // at xb[gi + mis].  Every bulk copy then starts and ends on 16 bytes.
+    const uint32_t mis = (uint32_t)((reinterpret_cast<uintptr_t>(a.x) & 15u) >> 2);
+    const float* xb = a.x - mis;
+
+    if (warp == 13) {
+        // ---------------- producer: one bulk copy of each tile's input span
+        if (lane == 0) {
+            uint32_t issued[2] = {0, 0};
+            for (uint64_t i = 0; i < cnt && !*abort_flag; ++i) {
+                const int r = (int)(i & 1);
+                const uint32_t use = (uint32_t)(i >> 1);
+                if (i >= 2 && !mbar_wait_t(&bar[B_RAW_EMPTY + r], (use - 1) & 1, abort_flag)) {
+                    give_up();
+                    break;
+                }
+                const uint64_t f0 = tile_of(i) * FPT;
+                const uint64_t nf = (a.frames - f0) < (uint64_t)FPT ? (a.frames - f0) : (uint64_t)FPT;
+                // virtual (xb-relative) span [a0, e16) of the tile, 16-byte granular;
+                // the loaders read the few samples past e16 from global memory
+                const uint64_t s0 = f0 * a.hop + mis;
+                const uint64_t a0 = s0 & ~(uint64_t)3;
+                uint64_t send = (f0 + nf - 1) * a.hop + N;
+                if (send > a.n) send = a.n;
+                send += mis;
+                const uint64_t e16 = send > a0 ? a0 + ((send - a0) & ~(uint64_t)3) : a0;
+                raw_base[r] = a0;
+                raw_end[r] = e16;
+                const uint32_t bytes = (uint32_t)((e16 - a0) * 4);
+                if (test_stall && i == 0) continue;  // test hook: nothing ever completes this phase
+                if (bytes) {
+                    mbar_expect_tx(&bar[B_RAW_FULL + r], bytes);
+                    bulk_g2s(RAW + r * (C::RAW_BYTES / 4), xb + a0, bytes, &bar[B_RAW_FULL + r]);
+                } else {
+                    mbar_arrive(&bar[B_RAW_FULL + r]);
+                }
+                ++issued[r];
+            }
+            // no copy may still be landing in shared memory when the CTA exits
+            for (int r = 0; r < 2; ++r)
+                if (issued[r]) mbar_wait_t(&bar[B_RAW_FULL + r], (issued[r] - 1) & 1, nullptr);
+        }
+    } else if (warp == 12) {
+        // ---------------- MMA issuer: MMA1(i), then MMA2(i-1)
+        if (lane == 0) {
+            const uint32_t b1 = smem_u32(sm + C::OFF_B1), b2 = smem_u32(sm + C::OFF_B2);
+            for (uint64_t i = 0; i <= cnt && !*abort_flag; ++i) {
+                if (i < cnt) {
+                    const int s = (int)(i & 1);
+                    const uint32_t use = (uint32_t)(i >> 1);
+                    if (!mbar_wait_t(&bar[B_A1_FULL + s], use & 1, abort_flag) ||
+                        (i >= 2 && !mbar_wait_t(&bar[B_D1_EMPTY + s], (use - 1) & 1, abort_flag))) {
+                        give_up();
+                        break;
+                    }
+                    for (int q = 0; q < FPT; ++q) sB[s * FPT + q] = sA[s * FPT + q];
+                    fence_after();
+                    const uint32_t a1 = smem_u32(A1 + s * C::A1_BYTES);
+                    const uint32_t d1 = tmem + s * C::NO;
+#pragma unroll
+                    for (int ks = 0; ks < C::K1 / 16; ++ks) {
+                        const uint64_t ah = sdesc(a1 + ks * 4096, 1024, 2048);
+                        const uint64_t al = sdesc(a1 + C::A1_BYTES / 2 + ks * 4096, 1024, 2048);
+                        const uint64_t bh = sdesc(b1 + ks * 32, 16, 1024);
+                        const uint64_t bl = sdesc(b1 + C::B1_BYTES / 2 + ks * 32, 16, 1024);
+                        mma_f16(d1, ah, bh, ID, ks > 0);
+                        mma_f16(d1, ah, bl, ID, 1);
+                        mma_f16(d1, al, bh, ID, 1);
+                    }
+                    mma_commit(&bar[B_A1_EMPTY + s]);
+                    mma_commit(&bar[B_D1_FULL + s]);
+                    mbar_arrive(&bar[B_D1_FULL + s]);
+                }
+                if (i >= 1) {
+                    const uint64_t j = i - 1;
+                    const int s = (int)(j & 1);
+                    const uint32_t use = (uint32_t)(j >> 1);
+                    if (!mbar_wait_t(&bar[B_A2_FULL + s], use & 1, abort_flag) ||
+                        (j >= 2 && !mbar_wait_t(&bar[B_D2_EMPTY + s], (use - 1) & 1, abort_flag))) {
+                        give_up();
+                        break;
+                    }
+                    for (int q = 0; q < FPT; ++q) sD[s * FPT + q] = sC[s * FPT + q];
+                    fence_after();
+                    const uint32_t a2 = smem_u32(A2 + s * C::A2_BYTES);
+                    const uint32_t d2 = tmem + 2 * C::NO + s * C::NO;
+#pragma unroll
+                    for (int ks = 0; ks < C::K2 / 16; ++ks) {
+                        const uint64_t ah = sdesc(a2 + ks * 4096, 1024, 2048);
+                        const uint64_t al = sdesc(a2 + C::A2_BYTES / 2 + ks * 4096, 1024, 2048);
+                        const uint64_t bh = sdesc(b2 + ks * 32, 16, 1024);
+                        const uint64_t bl = sdesc(b2 + C::B2_BYTES / 2 + ks * 32, 16, 1024);
+                        mma_f16(d2, ah, bh, ID, ks > 0);
+                        mma_f16(d2, ah, bl, ID, 1);
+                        mma_f16(d2, al, bh, ID, 1);
+                    }
+                    mma_commit(&bar[B_A2_EMPTY + s]);
+                    mma_commit(&bar[B_D2_FULL + s]);
+                    mbar_arrive(&bar[B_D2_FULL + s]);
+                }
+            }
+            // every MMA of this CTA has finished before tensor memory is released
+            mma_commit(&bar[B_FIN]);
+            mbar_wait_t(&bar[B_FIN], 0, nullptr);
+        }
+    } else if (warp < 4) {
+        // ---------------- loaders: window, DC, scale, split -> A1[s]
+        for (uint64_t i = 0; i < cnt; ++i) {
+            const int s = (int)(i & 1);
+            const uint32_t use = (uint32_t)(i >> 1);
+            bool ok = mbar_wait_t(&bar[B_RAW_FULL + s], use & 1, abort_flag);
+            if (ok && i >= 2) ok = mbar_wait_t(&bar[B_A1_EMPTY + s], (use - 1) & 1, abort_flag);
+            // one decision per warp: the shuffles below need every lane
+            if (!__all_sync(0xffffffffu, ok && !*abort_flag)) {
+                give_up();
+                break;
+            }
+            const uint64_t f0 = tile_of(i) * FPT;
+            const uint64_t a0 = raw_base[s], e16 = raw_end[s];
+            const float* raw = RAW + s * (C::RAW_BYTES / 4);
+            unsigned char* a1 = A1 + s * C::A1_BYTES;
+            for (int lf = warp; lf < FPT; lf += 4) {
+                const uint64_t f = f0 + lf;
+                const bool act = f < a.frames;
+                const uint64_t sb = f * a.hop + mis;  // virtual start of the frame
+                float x[N / 32];
+                // fast: the whole frame is staged and starts on a 16-byte word
+                const bool fast = act && sb + N <= e16 && ((sb - a0) & 3) == 0;
+#pragma unroll
+                for (int j = 0; j < N / 256; ++j) {  // lane owns samples [8c, 8c+8), c = lane + 32 j
+                    const int c = lane + 32 * j;
+                    if (fast) {
+                        const float4 p = *reinterpret_cast<const float4*>(raw + (sb - a0) + 8 * c);
+                        const float4 q = *reinterpret_cast<const float4*>(raw + (sb - a0) + 8 * c + 4);
+                        x[8 * j + 0] = p.x; x[8 * j + 1] = p.y; x[8 * j + 2] = p.z; x[8 * j + 3] = p.w;
+                        x[8 * j + 4] = q.x; x[8 * j + 5] = q.y; x[8 * j + 6] = q.z; x[8 * j + 7] = q.w;
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) {
+                            const uint64_t vi = sb + 8 * c + q;  // sample vi - mis
+                            float v = 0.0f;
+                            if (act && vi < a.n + mis) v = vi < e16 ? raw[vi - a0] : xb[vi];
+                            x[8 * j + q] = v;
+                        }
+                    }
+                }
+                float sum = 0.0f;
+#pragma unroll
+                for (int j = 0; j < N / 256; ++j) {
+                    const float4 w0 = *reinterpret_cast<const float4*>(WIN + ((2 * j) * 32 + lane) * 4);
+                    const float4 w1 = *reinterpret_cast<const float4*>(WIN + ((2 * j + 1) * 32 + lane) * 4);
+                    const float wv[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        x[8 * j + q] *= wv[q];
+                        sum += x[8 * j + q];
+                    }
+                }
+                if (a.remove_dc) {
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+                    const float mean = sum * (1.0f / (float)N);
+#pragma unroll
+                    for (int q = 0; q < N / 32; ++q) x[q] -= mean;
+                }
+                float mx = 0.0f;
+#pragma unroll
+                for (int q = 0; q < N / 32; ++q) mx = fmaxf(mx, fabsf(x[q]));
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+                int e2 = 0;
+                if (mx > 0.0f) frexpf(mx, &e2);  // mx in [2^(e2-1), 2^e2)
+                const float sc = ldexpf(1.0f, 14 - e2);
+                if (lane == 0) sA[s * FPT + lf] = ldexpf(1.0f, e2 - 14);
+#pragma unroll
+                for (int j = 0; j < N / 256; ++j) {
+                    const int c = lane + 32 * j;
+                    float v[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) v[q] = x[8 * j + q] * sc;
+                    uint4 hi, lo;
+                    split8p(v, hi, lo);
+                    // samples 8c..8c+7 = (g0..g0+7, m) with g = i mod R, m = i / R
+                    const int i0 = 8 * c, m = i0 / R, g0 = i0 % R;
+                    const uint32_t dst = mn_off(lf * R + g0, m);
+                    *reinterpret_cast<uint4*>(a1 + dst) = hi;
+                    *reinterpret_cast<uint4*>(a1 + C::A1_BYTES / 2 + dst) = lo;
+                }
+            }
+            mbar_arrive(&bar[B_RAW_EMPTY + s]);
+            fence_async_smem();
+            mbar_arrive(&bar[B_A1_FULL + s]);
+        }
+    } else if (warp < 8) {
+        // ---------------- epilogue 1: row = TMEM lane = (frame, g)
+        const int row = tid - 128, lf = row / R, g = row % R;
+        const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+        for (uint64_t i = 0; i < cnt; ++i) {
+            const int s = (int)(i & 1);
+            const uint32_t use = (uint32_t)(i >> 1);
+            const bool ok = mbar_wait_t(&bar[B_D1_FULL + s], use & 1, abort_flag);
+            if (!__all_sync(0xffffffffu, ok && !*abort_flag)) {
+                give_up();
+                break;
+            }
+            fence_after();
+            const float scale = sB[s * FPT + lf];
+            float y[C::NO];
+#pragma unroll
+            for (int cb = 0; cb < C::NO / 32; ++cb) {
+                float t[32];
+                tmem_ld32(tmem + s * C::NO + lane_base + cb * 32, t);
+#pragma unroll
+                for (int q = 0; q < 32; ++q) y[cb * 32 + q] = t[q];
+            }
+            fence_before();
+            mbar_arrive(&bar[B_D1_EMPTY + s]);
+            const bool ok2 = i < 2 || mbar_wait_t(&bar[B_A2_EMPTY + s], (use - 1) & 1, abort_flag);
+            if (!__all_sync(0xffffffffu, ok2)) {
+                give_up();
+                break;
+            }
+            if (g == 0) sC[s * FPT + lf] = scale;
+            unsigned char* a2 = A2 + s * C::A2_BYTES;
+#pragma unroll
+            for (int k1b = 0; k1b < R; k1b += 8) {
+                float re[8], im[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const int k1 = k1b + q;
+                    const float2 w = TW[k1 * R + g];  // W_N^{g k1} / R
+                    const float yr = y[2 * k1], yi = y[2 * k1 + 1];
+                    re[q] = yr * w.x - yi * w.y;
+                    im[q] = yr * w.y + yi * w.x;
+                }
+                uint4 hr, lr, hi_, li_;
+                split8p(re, hr, lr);
+                split8p(im, hi_, li_);
+                const uint32_t or_ = mn_off(lf * R + k1b, g);
+                const uint32_t oi_ = mn_off(lf * R + k1b, R + g);
+                *reinterpret_cast<uint4*>(a2 + or_) = hr;
+                *reinterpret_cast<uint4*>(a2 + C::A2_BYTES / 2 + or_) = lr;
+                *reinterpret_cast<uint4*>(a2 + oi_) = hi_;
+                *reinterpret_cast<uint4*>(a2 + C::A2_BYTES / 2 + oi_) = li_;
+            }
+            fence_async_smem();
+            mbar_arrive(&bar[B_A2_FULL + s]);
+        }
+    } else {
+        // ---------------- epilogue 2: row = TMEM lane = (frame, k1), holds X[k1 + R k2]
+        const int row = tid - 256, lf = row / R, k1 = row % R;
+        const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+        for (uint64_t j = 0; j < cnt; ++j) {
+            const int s = (int)(j & 1);
+            const uint32_t use = (uint32_t)(j >> 1);
+            const bool ok = mbar_wait_t(&bar[B_D2_FULL + s], use & 1, abort_flag);
+            if (!__all_sync(0xffffffffu, ok && !*abort_flag)) {
+                give_up();
+                break;
+            }
+            fence_after();
+            const float back = sD[s * FPT + lf] * (float)R;  // undo both scalings (powers of two)
+            float xs[C::NO];
+#pragma unroll
+            for (int cb = 0; cb < C::NO / 32; ++cb) {
+                float t[32];
+                tmem_ld32(tmem + 2 * C::NO + s * C::NO + lane_base + cb * 32, t);
+#pragma unroll
+                for (int q = 0; q < 32; ++q) xs[cb * 32 + q] = t[q];
+            }
+            fence_before();
+            mbar_arrive(&bar[B_D2_EMPTY + s]);
+            const uint64_t f = tile_of(j) * FPT + lf;
+            if (f < a.frames) {
+                if constexpr (OUTK == OUT_HALF) {
+                    float2* o2 = reinterpret_cast<float2*>(a.out);
+#pragma unroll
+                    for (int k2 = 0; k2 < R; ++k2) {
+                        const int k = k1 + R * k2;
+                        const float2 X = make_float2(xs[2 * k2] * back, xs[2 * k2 + 1] * back);
+                        if (!a.dense) {
+                            const uint64_t flat = f * (uint64_t)N + k;
+                            if (flat < a.ohalf) __stcs(o2 + flat, X);
+                        } else if (k <= N / 2) {
+                            __stcs(o2 + f * (uint64_t)(N / 2 + 1) + k, X);
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int k2 = 0; k2 <= R / 2; ++k2) {
+                        const int k = k1 + R * k2;
+                        if (k > N / 2) continue;
+                        const float xr = xs[2 * k2] * back, xi = xs[2 * k2 + 1] * back;
+                        const float p = (OUTK == OUT_POWER_SERIAL) ? fabsf(xr) * 1.41421356237309505f
+                                                                   : sqrtf(xr * xr + xi * xi);
+                        if (!a.dense) {
+                            float* rowp = a.out + f * (uint64_t)N;
+                            __stcs(rowp + k, p);
+                            if (k != 0 && k != N / 2) __stcs(rowp + (N - k), p);
+                        } else {
+                            __stcs(a.out + f * (uint64_t)(N / 2 + 1) + k, p);
+                        }
+                    }
+                }
+            }
+        }
+    }
+    __syncwarp();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 12) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(C::TMEM_COLS));
+    }
+}
+
+template <int R>
+const unsigned char* tc_tables(cudaError_t* e)
+{
+    // built once per process (one device per runner context)
+    static std::once_flag once;
+    static cudaError_t built = cudaSuccess;
+    static unsigned char* img = nullptr;
+    std::call_once(once, [&] {
+        void* p = nullptr;
+        if constexpr (R == 16) built = cudaGetSymbolAddress(&p, g_tc_tab16);
+        else built = cudaGetSymbolAddress(&p, g_tc_tab32);
+        if (built != cudaSuccess) return;
+        img = static_cast<unsigned char*>(p);
+        // a private stream: the caller's may be capturing a graph
+        cudaStream_t s2 = nullptr;
+        built = cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking);
+        if (built != cudaSuccess) return;
+        build_tc_tables_kernel<R><<<8, 256, 0, s2>>>(img);
+        built = cudaGetLastError();
+        if (built == cudaSuccess) built = cudaStreamSynchronize(s2);
+        cudaStreamDestroy(s2);
+    });
+    *e = built;
+    return img;
+}
+
+template <int R, int OUTK>
+cudaError_t launch_tc2_t(const FusedArgs& a, int* err, int test_stall, int sms, cudaStream_t st)
+{
+    using C = Tc2Cfg<R>;
+    cudaError_t e = cudaSuccess;
+    const unsigned char* tab = tc_tables<R>(&e);
+    if (e != cudaSuccess) return e;
+    auto k = stft_tc2_kernel<R, OUTK>;
+    static bool attr = false;
+    if (!attr) {
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    // one CTA per SM: its tensor memory (TMEM_COLS) and shared memory
+    const uint64_t ntiles = (a.frames + C::FPT - 1) / C::FPT;
+    const uint64_t grid = ntiles < (uint64_t)sms ? ntiles : (uint64_t)sms;
+    k<<<(unsigned)(grid ? grid : 1), kTc2Threads, C::SMEM, st>>>(a, tab, err, test_stall);
+    return cudaGetLastError();
 }
 
 template <int R, int OUTK>
@@ -462,8 +1052,20 @@ cudaError_t launch_tc_t(const FusedArgs& a, int* err, int sms, cudaStream_t st)
 
 bool tc_supports(int exp) { return exp == 8 || exp == 10; }
 
-cudaError_t launch_tc(int exp, int outk, const FusedArgs& a, int* err, int sms, cudaStream_t st)
+cudaError_t launch_tc(int exp, int outk, const FusedArgs& a, int* err, int test_stall, int sms, cudaStream_t st)
 {
+    // the pipelined form stages one tile's input span, sized for hop <= N
+    const bool piped = a.hop <= (1ull << exp) && (reinterpret_cast<uintptr_t>(a.x) & 3u) == 0;
+    if (piped && exp == 8) {
+        if (outk == OUT_HALF) return launch_tc2_t<16, OUT_HALF>(a, err, test_stall, sms, st);
+        if (outk == OUT_POWER_SERIAL) return launch_tc2_t<16, OUT_POWER_SERIAL>(a, err, test_stall, sms, st);
+        return launch_tc2_t<16, OUT_POWER>(a, err, test_stall, sms, st);
+    }
+    if (piped && exp == 10) {
+        if (outk == OUT_HALF) return launch_tc2_t<32, OUT_HALF>(a, err, test_stall, sms, st);
+        if (outk == OUT_POWER_SERIAL) return launch_tc2_t<32, OUT_POWER_SERIAL>(a, err, test_stall, sms, st);
+        return launch_tc2_t<32, OUT_POWER>(a, err, test_stall, sms, st);
+    }
     if (exp == 8) {
         if (outk == OUT_HALF) return launch_tc_t<16, OUT_HALF>(a, err, sms, st);
         if (outk == OUT_POWER_SERIAL) return launch_tc_t<16, OUT_POWER_SERIAL>(a, err, sms, st);

@@ -43,3 +43,88 @@ def test_tc_scaling_extremes(ocs_lib, orc):
 def test_tc_rejects_unsupported_window(ocs_lib):
     with pytest.raises(ocs_lib.OcsError):
         ocs_lib.activate(signal(1, 10000), 9, 0.5, "--precision=tc-fp16")
+
+
+@pytest.mark.parametrize("exp", [8, 10])
+def test_tc_many_tiles_per_cta(ocs_lib, orc, exp):
+    """Long signals: every CTA runs many tiles, so each double buffer is
+    reused many times (phase parity of every pipeline barrier wraps)."""
+    x = signal(900 + exp, 3_000_017)
+    for opts in ("--hanning_window --remove_dc", "--blackman_window --half_complex_return --layout=dense"):
+        got = ocs_lib.activate(x, exp, 0.75, opts + " --precision=tc-fp16")
+        ref = orc.fp64_stft(x, exp, 0.75, opts)
+        assert orc.rel_l2(got, ref) <= REL_L2, (exp, opts)
+
+
+@pytest.mark.parametrize("shift", [1, 2, 3, 5])
+def test_tc_unaligned_device_input(ocs_lib, orc, shift):
+    """Signal pointers that are not 16-byte aligned (offset by whole floats)."""
+    import torch
+    exp, ov, opts = 10, 0.75, "--hamming_window --remove_dc --layout=dense"
+    x = signal(31 + shift, 200_003)
+    g = ocs_lib.geometry(x.size, exp, ov, opts)
+    buf = torch.zeros(x.size + 8, dtype=torch.float32, device="cuda")
+    buf[shift:shift + x.size] = torch.from_numpy(x).cuda()
+    d_out = torch.empty(g.out_floats, dtype=torch.float32, device="cuda")
+    ocs_lib.activate_device(buf[shift:].data_ptr(), x.size, exp, ov, opts + " --precision=tc-fp16", d_out,
+                            g.out_floats)
+    torch.cuda.synchronize()
+    ref = orc.fp64_stft(x, exp, ov, opts)
+    assert orc.rel_l2(d_out.cpu().numpy(), ref) <= REL_L2
+
+
+def test_tc_hop_longer_than_window(ocs_lib, orc):
+    """Negative overlap (frame advance above the window) takes the
+    non-pipelined tensor-core kernel."""
+    x = signal(8, 100_000)
+    for exp in (8, 10):
+        got = ocs_lib.activate(x, exp, -0.5, "--hanning_window --precision=tc-fp16")
+        ref = orc.fp64_stft(x, exp, -0.5, "--hanning_window")
+        assert orc.rel_l2(got, ref) <= REL_L2, exp
+
+
+STALL_CHILD = r'''
+import sys
+import numpy as np
+sys.path.insert(0, {root!r})
+import occastft_gb300 as ocs
+from oracle import orc
+x = np.random.default_rng(3).uniform(-1, 1, 400_000).astype(np.float32)
+try:
+    ocs.activate(x, 10, 0.75, "--hanning_window --precision=tc-fp16")
+    print("NO-ERROR")
+except ocs.OcsError as e:
+    print("CODE", e.code)
+got = ocs.activate(x, 10, 0.75, "--hanning_window")
+print("AFTER", orc.rel_l2(got, orc.fp64_stft(x, 10, 0.75, "--hanning_window")))
+'''
+
+
+def test_tc_wait_timeout_reports_error():
+    """Every pipeline wait of the tensor-core kernel is bounded: with the test
+    hook the first input phase never completes, the waits give up after about
+    a second, the call returns OCS_ETIMEDOUT and the context stays usable."""
+    import os
+    import subprocess
+    import sys
+    from tests.conftest import ROOT
+    e = dict(os.environ)
+    e["OCS_TC_TEST_STALL"] = "1"
+    out = subprocess.run([sys.executable, "-c", STALL_CHILD.format(root=ROOT)], env=e, capture_output=True,
+                         text=True, timeout=300)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = out.stdout.strip().splitlines()
+    assert "CODE 6" in lines, lines
+    after = float([ln for ln in lines if ln.startswith("AFTER")][0].split()[1])
+    assert after <= REL_L2
+
+
+@pytest.mark.parametrize("exp,ov", [(8, 0.3), (10, 0.33), (10, 0.1), (8, 0.0)])
+def test_tc_odd_hop(ocs_lib, orc, exp, ov):
+    """Frame advances that are not a multiple of four samples: frames start
+    at every offset inside a 16-byte word of the staged input."""
+    x = signal(400 + exp, 123_457)
+    for opts in ("--hanning_window --remove_dc", "--blackman_window --half_complex_return"):
+        got = ocs_lib.activate(x, exp, ov, opts + " --precision=tc-fp16")
+        ref = orc.fp64_stft(x, exp, ov, opts)
+        assert orc.rel_l2(got, ref) <= REL_L2, (exp, ov, opts)
