@@ -19,6 +19,10 @@ OUT_DIR = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libocs_gb300.so")
 RUNNER_LIB = os.path.join(PKG, "libocs_runner.so")
 RUNNER_DEMO = os.path.join(PKG, "ocs_runner_demo")
+STANDALONE = os.path.join(PKG, "standalone")
+# the runner executable the reference's proxy launches (`<dir>/cudaRun <port>`)
+CUDARUN = os.path.join(PKG, "cudaRun")
+STANDALONE_SOURCES = ["request_codec.cpp", "ws_server.cpp", "shm_payload.cpp", "cudaRun.cpp"]
 
 CU_SOURCES = ["stft_fused.cu", "stft_fused_lo.cu", "stft_fused_hi.cu", "stft_pair_lo.cu", "stft_pair_hi.cu",
               "stft_batch.cu", "stft_batch_noalloc.cu", "stft_tc.cu", "stft_stages.cu"]
@@ -87,6 +91,17 @@ def build(verbose: bool = False, force: bool = False) -> str:
         runner_objs.append(o)
         if force or _stale(o, [s] + headers):
             jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-Wall", *inc, "-I", RUNNER, "-c", s, "-o", o])
+    sa_objs = []
+    sa_headers = [os.path.join(STANDALONE, f) for f in os.listdir(STANDALONE) if f.endswith(".hpp")] \
+        if os.path.isdir(STANDALONE) else []
+    for f in STANDALONE_SOURCES:
+        s = os.path.join(STANDALONE, f)
+        if not os.path.exists(s):
+            continue
+        o = os.path.join(OUT_DIR, "sa_" + f + ".o")
+        sa_objs.append(o)
+        if force or _stale(o, [s] + headers + sa_headers):
+            jobs.append(["g++", "-std=c++17", "-O2", "-Wall", *inc, "-I", STANDALONE, "-c", s, "-o", o])
     log = []
     with ThreadPoolExecutor(max_workers=max(2, min(8, os.cpu_count() or 2))) as ex:
         for out in ex.map(_run, jobs):
@@ -106,6 +121,9 @@ def build(verbose: bool = False, force: bool = False) -> str:
             _run(["g++", "-std=c++17", "-O2", *inc, "-I", RUNNER, demo_src, "-o", RUNNER_DEMO, "-L", PKG,
                   "-locs_runner", "-locs_gb300", "-L", libdir, "-lcudart", "-Wl,-rpath,$ORIGIN",
                   "-Wl,-rpath," + libdir])
+    if sa_objs and (force or jobs or not os.path.exists(CUDARUN)):
+        _run(["g++", "-o", CUDARUN, *sa_objs, "-L", PKG, "-locs_gb300", "-L", libdir, "-lcudart", "-lpthread",
+              "-lrt", "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + libdir])
     if verbose:
         print("\n".join(l for l in log if l.strip()))
     return LIB
