@@ -390,6 +390,80 @@ def draw_served(rng, count):
     return lens, exps, ovs, opts
 
 
+def run_runner_leg(ocs, x_host, n, reps=5, warmup=2, env=None):
+    """The drop-in runner executable end to end: occastft_gb300/cudaRun
+    serving RequestCapnp messages over a WebSocket with the signal in POSIX
+    shared memory (the reference proxy's local-runner path).  Timed per
+    request from send to answer; the proxy's refill of the shared memory
+    with the signal (the runner writes its result over it) is outside."""
+    import socket
+    import subprocess
+
+    from occastft_gb300 import proxy, wire
+
+    exe = os.path.join(ROOT, "occastft_gb300", "cudaRun")
+    if not os.path.exists(exe):
+        return {"unavailable": "cudaRun not built"}
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    penv = dict(os.environ)
+    penv.update(env or {})
+    p = subprocess.Popen([exe, str(port)], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL, env=penv)
+    shm = None
+    ws = None
+    try:
+        for _ in range(600):
+            try:
+                ws = proxy.WsClient("127.0.0.1", port, timeout=0.2)
+                break
+            except OSError:
+                time.sleep(0.1)
+        if ws is None:
+            return {"unavailable": "cudaRun did not accept a connection"}
+        olen = proxy.to_overlap_length(n, HEAD_OV, 1 << HEAD_EXP)
+        shm = proxy.SharedPayload("bench", olen)
+        view = shm.floats()
+        req = wire.Request(windowRadix=HEAD_EXP, overlapRatio=HEAD_OV, mappedID="bench", sharedMemory=shm.name,
+                           dataLength=n, overlapdataLength=olen, options=HEAD_OPTS, posixFileDes=-1)
+        msg = wire.encode(req)
+        times = []
+        for i in range(warmup + reps):
+            view[:n] = x_host
+            t0 = time.perf_counter()
+            ws.send_binary(msg)
+            op, payload = ws.recv(timeout=120)
+            dt = time.perf_counter() - t0
+            if op != 2 or wire.decode(payload).sharedMemory == "ERR":
+                return {"unavailable": "cudaRun answered ERR"}
+            if i >= warmup:
+                times.append(dt)
+        del view
+        ms = float(np.median(times)) * 1e3
+        return {"workload": f"{n} samples, window {1 << HEAD_EXP}, overlap {HEAD_OV}, '{HEAD_OPTS}', "
+                            "signal and result in one POSIX shared memory region",
+                "ms_per_request": round(ms, 3), "gsamples_s": round(n / ms / 1e6, 2), "requests": reps,
+                "bytes_in": n * 4, "bytes_out": olen * 4,
+                "note": "send-to-answer time of one request through the WebSocket protocol; the runner copies the "
+                        "signal to the device in chunks and writes each part of the result back once the input "
+                        "it overwrites has been copied"}
+    finally:
+        if ws is not None:
+            try:
+                ws.send_text("CLOSE_REQUEST")
+                ws.recv(timeout=10)
+            except Exception:  # noqa: BLE001
+                pass
+            ws.close()
+        if shm is not None:
+            shm.release()
+        try:
+            p.wait(timeout=20)
+        except subprocess.TimeoutExpired:
+            p.kill()
+            p.wait()
+
+
 def run_serving_leg(ocs, rates=(2000, 10000, 50000), durations=(1.0, 0.5, 0.3), seed=3):
     """Poisson request stream against the continuous-batching server (host buffers in and out),
     and the same draws served one at a time through ocs_activate."""
@@ -670,6 +744,9 @@ def run_ours(args):
     serving = None
     if rank == 0 and not args.no_serve:
         serving = run_serving_leg(ocs)
+    runner_exe = None
+    if rank == 0 and not args.no_serve:
+        runner_exe = run_runner_leg(ocs, x.cpu().numpy(), n)
 
     if rank != 0:
         if ws > 1:
@@ -703,6 +780,7 @@ def run_ours(args):
         "tensor_core": tc,
         "uneven_batch": batch,
         "serving": serving,
+        "runner_executable": runner_exe,
     }
     print(json.dumps(line))
     if ws > 1:

@@ -78,7 +78,9 @@ int ocs_geometry_get(uint64_t n, int window_size_exp, float overlap_ratio, const
 /* Runner::ActivateSTFT (RunnerInterface.hpp:124-128; CUDA version
  * CudaImpl.cpp:410-510): host signal in, host result out, synchronous.
  * out must hold geometry.out_floats floats; *out_len receives that count.
- * Host buffers from ocs_host_alloc give the fastest copies. */
+ * Host buffers from ocs_host_alloc give the fastest copies.  out may overlap
+ * in (the result written over the signal): each part of the result is copied
+ * back only after the input it overwrites has reached the device. */
 int ocs_activate(const float* in, uint64_t n, int window_size_exp, float overlap_ratio, const char* options,
                  float* out, uint64_t out_cap, uint64_t* out_len);
 
@@ -101,6 +103,12 @@ int ocs_window_table(int kind, uint32_t window_size, float sigma, float* out);
 /* Pinned host memory for inputs/outputs of ocs_activate. */
 int ocs_host_alloc(void** ptr, size_t bytes);
 int ocs_host_free(void* ptr);
+
+/* Pins an existing host range (a mapped shared-memory payload, say) for the
+ * copies of ocs_activate, and releases it again.  No counterpart in the
+ * reference, whose runners copy such payloads into new vectors first. */
+int ocs_host_register(void* ptr, size_t bytes);
+int ocs_host_unregister(void* ptr);
 
 /* ---- uneven batches: many requests, one persistent launch ---- */
 

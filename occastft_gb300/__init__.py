@@ -86,6 +86,8 @@ SIGNATURES = {
     "ocs_window_table": (ctypes.c_int, [ctypes.c_int, ctypes.c_uint32, ctypes.c_float, _VP]),
     "ocs_host_alloc": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t]),
     "ocs_host_free": (ctypes.c_int, [_VP]),
+    "ocs_host_register": (ctypes.c_int, [_VP, ctypes.c_size_t]),
+    "ocs_host_unregister": (ctypes.c_int, [_VP]),
     "ocs_batch_prepare": (ctypes.c_int, [_VP, ctypes.c_int]),
     "ocs_batch_device": (ctypes.c_int, [_VP, ctypes.c_int, _VP]),
     "ocs_batch_device_noalloc": (ctypes.c_int, [_VP, ctypes.c_int, _VP]),

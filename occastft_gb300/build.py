@@ -122,8 +122,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
                   "-locs_runner", "-locs_gb300", "-L", libdir, "-lcudart", "-Wl,-rpath,$ORIGIN",
                   "-Wl,-rpath," + libdir])
     if sa_objs and (force or jobs or not os.path.exists(CUDARUN)):
-        _run(["g++", "-o", CUDARUN, *sa_objs, "-L", PKG, "-locs_gb300", "-L", libdir, "-lcudart", "-lpthread",
-              "-lrt", "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + libdir])
+        _run(["g++", "-o", CUDARUN, *sa_objs, "-L", PKG, "-locs_gb300", "-lpthread", "-lrt", "-Wl,-rpath,$ORIGIN"])
     if verbose:
         print("\n".join(l for l in log if l.strip()))
     return LIB

@@ -836,17 +836,36 @@ int ocs_activate(const float* in, uint64_t n, int exp, float ov, const char* opt
     uint64_t chunks = std::min<uint64_t>(kMaxChunks, std::max<uint64_t>(1, (F + target - 1) / target));
     const uint64_t per = (F + chunks - 1) / chunks;
     chunks = (F + per - 1) / per;
+    // Input prefix copied once chunk ci's host-to-device copy has finished.
+    std::vector<uint64_t> in_hi(chunks);
+    for (uint64_t ci = 0; ci < chunks; ++ci) {
+        const uint64_t f1 = std::min(F, ci * per + per);
+        in_hi[ci] = std::min<uint64_t>(need_in, (f1 - 1) * hop + N);
+    }
+    // In-place use (out overlapping in, e.g. a shared-memory region that
+    // holds the signal and receives the result): a device-to-host copy may
+    // only overwrite input that has already reached the device, so it also
+    // waits for the first host-to-device chunk that covers the input it
+    // overlaps.  All input copies are issued first in that case.
+    const uintptr_t ib = reinterpret_cast<uintptr_t>(in), ie = ib + need_in * sizeof(float);
+    const uintptr_t ob = reinterpret_cast<uintptr_t>(out), oe = ob + r.geo.out_floats * sizeof(float);
+    const bool aliased = ob < ie && ib < oe;
     uint64_t copied = 0;
     cudaError_t e = cudaSuccess;
-    for (uint64_t ci = 0; ci < chunks && e == cudaSuccess; ++ci) {
-        const uint64_t f0 = ci * per, f1 = std::min(F, f0 + per);
-        const uint64_t hi = std::min<uint64_t>(need_in, (f1 - 1) * hop + N);
+    auto issue_h2d = [&](uint64_t ci) {
+        const uint64_t hi = in_hi[ci];
         if (hi > copied) {
             e = cudaMemcpyAsync(s->d_in + copied, in + copied, (hi - copied) * sizeof(float), cudaMemcpyHostToDevice,
                                 s->s_h2d);
             copied = hi;
         }
         if (e == cudaSuccess) e = cudaEventRecord(s->ev_in[ci], s->s_h2d);
+    };
+    if (aliased)
+        for (uint64_t ci = 0; ci < chunks && e == cudaSuccess; ++ci) issue_h2d(ci);
+    for (uint64_t ci = 0; ci < chunks && e == cudaSuccess; ++ci) {
+        const uint64_t f0 = ci * per, f1 = std::min(F, f0 + per);
+        if (!aliased) issue_h2d(ci);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s->s_comp, s->ev_in[ci], 0);
         if (e != cudaSuccess) break;
         rc = launch_frames(r, s->d_in, need_in, s->d_out, f0, f1, s->s_comp);
@@ -855,6 +874,15 @@ int ocs_activate(const float* in, uint64_t n, int exp, float ov, const char* opt
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s->s_d2h, s->ev_comp[ci], 0);
         uint64_t off, cnt;
         out_range(r, f0, f1, &off, &cnt);
+        if (e == cudaSuccess && aliased && cnt) {
+            const uintptr_t wb = ob + off * sizeof(float), we = wb + cnt * sizeof(float);
+            if (wb < ie && ib < we) {
+                const uint64_t need = (std::min(we, ie) - ib + sizeof(float) - 1) / sizeof(float);
+                uint64_t cj = ci;
+                while (cj + 1 < chunks && in_hi[cj] < need) ++cj;
+                if (cj > ci) e = cudaStreamWaitEvent(s->s_d2h, s->ev_in[cj], 0);
+            }
+        }
         if (e == cudaSuccess && cnt)
             e = cudaMemcpyAsync(out + off, s->d_out + off, cnt * sizeof(float), cudaMemcpyDeviceToHost, s->s_d2h);
     }
@@ -895,6 +923,21 @@ int ocs_host_alloc(void** ptr, size_t bytes)
 int ocs_host_free(void* ptr)
 {
     OCS_CUDA(cudaFreeHost(ptr));
+    return OCS_OK;
+}
+
+int ocs_host_register(void* ptr, size_t bytes)
+{
+    if (!ptr || !bytes) return fail(OCS_EINVAL, "host register: empty range");
+    int rc = ensure_init();
+    if (rc) return rc;
+    OCS_CUDA(cudaHostRegister(ptr, bytes, cudaHostRegisterPortable));
+    return OCS_OK;
+}
+
+int ocs_host_unregister(void* ptr)
+{
+    OCS_CUDA(cudaHostUnregister(ptr));
     return OCS_OK;
 }
 

@@ -7,19 +7,11 @@
 // instead of the reference's allocate / copy / seven launches / copy / free.
 // Like the CUDA runner it returns std::nullopt when the pipeline status is not
 // "OK" (CudaImpl.cpp:497-501); the status is kept in last_status.
-#include "occastft_runner.hpp"
+#include "gb300Struct.hpp"
 #include "occastft_gb300.h"
+#include "occastft_runner.hpp"
 
 #include <cstdlib>
-
-struct Genv {
-    int device = 0;
-};
-
-struct Gcodes {
-    // the fused kernels are compiled ahead of time for sm_103a; plans (twiddle
-    // and window tables, launch shapes) are built on first use and cached
-};
 
 void Runner::InitEnv()
 {

@@ -4,6 +4,7 @@
 // provides these (with its WebSocket server); this file restates the
 // pipeline's stage order and option handling (RunnerCommon.cpp:166-316) so the
 // hooks can be driven stage by stage here too.
+#include "gb300Struct.hpp"
 #include "occastft_runner.hpp"
 
 Runner::Runner(const int& portNumber)

@@ -18,8 +18,6 @@
 // that do not fit the shared memory region, or a data list longer than a
 // Cap'n Proto list can hold (2^29 - 1 elements), answer "ERR" instead of
 // writing past the region.
-#include <cuda_runtime.h>
-
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -38,66 +36,27 @@ namespace {
 
 bool g_log = false;
 
-// Device buffers and a stream per connection (requests of one connection run
-// in order, connections run concurrently).
-struct Worker {
-    cudaStream_t st = nullptr;
-    float* d_in = nullptr;
-    float* d_out = nullptr;
-    uint64_t in_cap = 0, out_cap = 0;
+// How a shared-memory payload is prepared for the device copies:
+// pin: page-locked for the request (cudaHostRegister), the default;
+// populate: page tables built at map time, copies through the driver's
+// pageable path; plain: neither.  OCS_CUDARUN_SHM=pin|populate|plain.
+enum class ShmMode { pin, populate, plain };
+ShmMode g_shm_mode = ShmMode::pin;
 
-    ~Worker()
-    {
-        if (d_in) cudaFree(d_in);
-        if (d_out) cudaFree(d_out);
-        if (st) cudaStreamDestroy(st);
-    }
-
-    static std::string cuda_err(cudaError_t e, const char* what)
-    {
-        return std::string(what) + ": " + cudaGetErrorString(e);
-    }
-
-    std::string grow(float** p, uint64_t* cap, uint64_t need)
-    {
-        if (need <= *cap) return "";
-        if (*p) cudaFree(*p);
-        *p = nullptr;
-        *cap = 0;
-        const cudaError_t e = cudaMalloc(p, need * sizeof(float));
-        if (e != cudaSuccess) return cuda_err(e, "cudaMalloc");
-        *cap = need;
-        return "";
-    }
-
-    // Runs the pipeline on host memory in, writing out.  The whole input
-    // reaches the device before any output is written back, so in and out may
-    // be the same region (the shared-memory case).
-    std::string run(const float* in, uint64_t n, int exp, float ov, const std::string& opts, float* out,
-                    uint64_t out_cap_floats, uint64_t* out_len)
-    {
-        ocs_geometry g;
-        if (ocs_geometry_get(n, exp, ov, opts.c_str(), &g) != OCS_OK) return ocs_last_error();
-        if (g.out_floats > out_cap_floats) return "result larger than the shared memory region";
-        if (!st) {
-            const cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
-            if (e != cudaSuccess) return cuda_err(e, "cudaStreamCreate");
-        }
-        std::string s = grow(&d_in, &in_cap, n);
-        if (s.empty()) s = grow(&d_out, &out_cap, g.out_floats);
-        if (!s.empty()) return s;
-        cudaError_t e = cudaMemcpyAsync(d_in, in, n * sizeof(float), cudaMemcpyHostToDevice, st);
-        if (e != cudaSuccess) return cuda_err(e, "cudaMemcpyAsync H2D");
-        if (ocs_activate_device(d_in, n, exp, ov, opts.c_str(), d_out, g.out_floats, st) != OCS_OK)
-            return ocs_last_error();
-        e = cudaMemcpyAsync(out, d_out, g.out_floats * sizeof(float), cudaMemcpyDeviceToHost, st);
-        if (e != cudaSuccess) return cuda_err(e, "cudaMemcpyAsync D2H");
-        e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) return cuda_err(e, "cudaStreamSynchronize");
-        *out_len = g.out_floats;
-        return "";
-    }
-};
+// Runs the pipeline on host memory through ocs_activate (copies in chunks,
+// overlapped with the kernels).  in and out may be the same region (the
+// shared-memory case): ocs_activate then writes each part of the result only
+// after the input it overwrites has reached the device.
+std::string run_pipeline(const float* in, uint64_t n, int exp, float ov, const std::string& opts, float* out,
+                         uint64_t out_cap_floats)
+{
+    ocs_geometry g;
+    if (ocs_geometry_get(n, exp, ov, opts.c_str(), &g) != OCS_OK) return ocs_last_error();
+    if (g.out_floats > out_cap_floats) return "result larger than the shared memory region";
+    uint64_t len = 0;
+    if (ocs_activate(in, n, exp, ov, opts.c_str(), out, out_cap_floats, &len) != OCS_OK) return ocs_last_error();
+    return "";
+}
 
 // the answer's fields: the request's, except options and data (MakeWField,
 // FFTStruct.cpp:95-110)
@@ -125,7 +84,7 @@ void send_answer(Connection& c, const Request& a)
 
 constexpr uint64_t kMaxListElements = (1ull << 29) - 1;
 
-void handle_request(Connection& c, const Message& m, Worker& w)
+void handle_request(Connection& c, const Message& m)
 {
     const auto t0 = std::chrono::steady_clock::now();
     Request q;
@@ -148,14 +107,17 @@ void handle_request(Connection& c, const Message& m, Worker& w)
             status = "request marked ERR";
         } else {
             ShmMapping map;
-            status = shm_map(q.sharedMemory, q.overlapdataLength, map);
+            status = shm_map(q.sharedMemory, q.overlapdataLength, map, g_shm_mode == ShmMode::populate);
             if (status.empty() && q.dataLength * sizeof(float) > map.bytes)
                 status = "dataLength floats exceed the shared memory region";
-            uint64_t len = 0;
+            bool pinned = false;
+            if (status.empty() && g_shm_mode == ShmMode::pin)
+                pinned = ocs_host_register(map.ptr, map.bytes) == OCS_OK;  // unpinned still works, slower
             if (status.empty()) {
                 float* p = static_cast<float*>(map.ptr);
-                status = w.run(p, q.dataLength, exp, q.overlapRatio, q.options, p, map.bytes / sizeof(float), &len);
+                status = run_pipeline(p, q.dataLength, exp, q.overlapRatio, q.options, p, map.bytes / sizeof(float));
             }
+            if (pinned) ocs_host_unregister(map.ptr);
             shm_unmap(map);
         }
         if (!status.empty()) a.sharedMemory = "ERR";
@@ -175,8 +137,7 @@ void handle_request(Connection& c, const Message& m, Worker& w)
             std::vector<uint64_t> buf((encoded_size(a) + 7) / 8);
             float* slot = nullptr;
             encode_request(a, reinterpret_cast<uint8_t*>(buf.data()), &slot);
-            uint64_t len = 0;
-            status = w.run(q.data, q.dataCount, exp, q.overlapRatio, q.options, slot, g.out_floats, &len);
+            status = run_pipeline(q.data, q.dataCount, exp, q.overlapRatio, q.options, slot, g.out_floats);
             if (status.empty()) c.send_binary(reinterpret_cast<const uint8_t*>(buf.data()), encoded_size(a));
         }
         if (!status.empty()) {
@@ -213,6 +174,10 @@ int main(int argc, char* argv[])
     }
     const char* lg = std::getenv("OCS_CUDARUN_LOG");
     g_log = lg && lg[0] == '1';
+    if (const char* sm = std::getenv("OCS_CUDARUN_SHM")) {
+        if (!std::strcmp(sm, "populate")) g_shm_mode = ShmMode::populate;
+        else if (!std::strcmp(sm, "plain")) g_shm_mode = ShmMode::plain;
+    }
     // listen first: a proxy may connect while the device initialises (its
     // connection waits in the backlog until the serve loop accepts it)
     WsServer server;
@@ -226,9 +191,8 @@ int main(int argc, char* argv[])
         std::fprintf(stderr, "cudaRun: device init failed (%s); requests will answer ERR\n", ocs_last_error());
     if (g_log) std::fprintf(stderr, "cudaRun: listening on 0.0.0.0:%d\n", server.port());
     server.run([&](Connection& c, const Message& m) {
-        thread_local Worker w;
         if (m.binary) {
-            handle_request(c, m, w);
+            handle_request(c, m);
         } else if (m.text() == "CLOSE_REQUEST") {
             c.send_text("CLOSE_COMPLETE");
             server.stop();

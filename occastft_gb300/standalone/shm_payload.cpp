@@ -18,7 +18,7 @@ size_t page_rounded_bytes(uint64_t floats)
     return (size_t)((bytes + page - 1) / page * page);
 }
 
-std::string shm_map(const std::string& name, uint64_t overlap_floats, ShmMapping& m)
+std::string shm_map(const std::string& name, uint64_t overlap_floats, ShmMapping& m, bool populate)
 {
     m = ShmMapping{};
     const size_t bytes = page_rounded_bytes(overlap_floats);
@@ -31,7 +31,9 @@ std::string shm_map(const std::string& name, uint64_t overlap_floats, ShmMapping
         close(fd);
         return "shared memory object " + name + " is smaller than overlapdataLength floats";
     }
-    void* p = mmap(nullptr, bytes, PROT_READ | PROT_WRITE, MAP_SHARED, fd, 0);
+    // MAP_POPULATE: build the page tables now, in one pass, instead of one
+    // fault per page while the copies to and from the device run over it
+    void* p = mmap(nullptr, bytes, PROT_READ | PROT_WRITE, MAP_SHARED | (populate ? MAP_POPULATE : 0), fd, 0);
     if (p == MAP_FAILED) {
         const std::string e = std::strerror(errno);
         close(fd);

@@ -22,8 +22,9 @@ struct ShmMapping {
 // page-rounded byte size of `floats` floats (FFTStruct.hpp:151-157)
 size_t page_rounded_bytes(uint64_t floats);
 
-// Opens and maps an existing object.  Returns "" or the error.
-std::string shm_map(const std::string& name, uint64_t overlap_floats, ShmMapping& m);
+// Opens and maps an existing object; `populate` builds the mapping's page
+// tables up front.  Returns "" or the error.
+std::string shm_map(const std::string& name, uint64_t overlap_floats, ShmMapping& m, bool populate);
 
 void shm_unmap(ShmMapping& m);
 
