@@ -757,14 +757,20 @@ def run_ours(args):
         return
 
     cpu = None if args.no_cpu else cpu_baseline()
-    traffic = load_traffic(f"stft_fused_e{HEAD_EXP}_hamming_power_1e8")
+    headline = (n == 100_000_000 and HEAD_EXP == 10 and HEAD_OV == 0.5 and HEAD_OPTS == "--hamming_window")
+    # the committed ncu traffic figure belongs to the headline workload only
+    traffic = load_traffic(f"stft_fused_e{HEAD_EXP}_hamming_power_1e8") if headline else None
+    if headline:
+        workload = ("fused STFT of a 1e8-sample float32 signal (8 seeded sinusoids + N(0,0.01^2), fs 48 kHz), "
+                    "window 1024 Hamming, overlap 0.5, power in the reference layout (qt x N floats)")
+    else:
+        workload = (f"fused STFT of a {n}-sample float32 signal (8 seeded sinusoids + N(0,0.01^2), fs 48 kHz), "
+                    f"window {1 << HEAD_EXP}, overlap {HEAD_OV}, options '{HEAD_OPTS}'")
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": METRIC, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(per_step * 1e3, 5), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "fused STFT of a 1e8-sample float32 signal (8 seeded sinusoids + N(0,0.01^2), "
-                               "fs 48 kHz), window 1024 Hamming, overlap 0.5, power in the reference layout "
-                               "(qt x N floats)", "samples": n, "window": 1 << HEAD_EXP, "overlap": HEAD_OV,
+        "config": {"workload": workload, "samples": n, "window": 1 << HEAD_EXP, "overlap": HEAD_OV,
                    "options": HEAD_OPTS, "frames": geo.qt, "l2_flush": "not needed: 1.2 GB per step > 129 MB L2",
                    "parallelism": f"replica x{ws} (frames shard with no exchange)"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
