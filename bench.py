@@ -600,8 +600,8 @@ def run_ours(args):
     n = N_SAMPLES
     x = make_signal_torch(n)
     geo = ocs.geometry(n, HEAD_EXP, HEAD_OV, HEAD_OPTS)
-    # room for the largest output of the sweep (window 2^15, overlap 0.5)
-    cap = max(geo.out_floats, ocs.geometry(n, 15, 0.5, "").out_floats)
+    # room for the largest output of the sweep (windows up to 2^22, overlap 0.5)
+    cap = max([geo.out_floats] + [ocs.geometry(n, e, 0.5, "").out_floats for e in range(6, 23)])
     d_out = torch.empty(cap, device="cuda")
     peak, peak_kind = load_peaks()
 
@@ -691,7 +691,7 @@ def run_ours(args):
     # the rest of the config: window sweep, device-resident
     sweep = []
     if rank == 0 and not args.no_sweep:
-        for exp in range(6, 16):
+        for exp in range(6, 23):
             for wname in ("hamming", "blackman"):
                 for out_kind in ("power", "half_complex"):
                     opts = f"--{wname}_window" + (" --half_complex_return" if out_kind == "half_complex" else "")

@@ -66,6 +66,7 @@ struct Context {
     cudaStream_t s_setup = nullptr;
     std::map<int, float2*> twiddles;                             // exp * 2 + paired -> table
     std::map<std::tuple<int, int, uint32_t>, float*> windows;    // (kind, exp, sigma bits) -> table
+    std::map<uint64_t, float2*> two_level;                       // L -> exp(-2 pi i j / L) lo|hi table
     std::map<std::pair<int, int>, int> occupancy;                // (exp, output kind) -> CTAs per SM
     std::vector<Slot*> free_slots;
     std::vector<Slot*> all_slots;
@@ -310,6 +311,71 @@ int ilog2u(uint64_t v)
     return l;
 }
 
+// exp(-2 pi i j / L) for j < L as lo[j % 1024] * hi[j / 1024]: 1024 + L/1024 entries
+int get_two_level(uint64_t L, const float2** lo, const float2** hi)
+{
+    Context& c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    auto it = c.two_level.find(L);
+    if (it == c.two_level.end()) {
+        float2* d = nullptr;
+        const uint64_t nhi = (L + 1023) / 1024;
+        OCS_CUDA(cudaMalloc(&d, sizeof(float2) * (1024 + nhi)));
+        OCS_CUDA(ocs::build_two_level(d, d + 1024, L, c.s_setup));
+        OCS_CUDA(cudaStreamSynchronize(c.s_setup));
+        it = c.two_level.emplace(L, d).first;
+    }
+    *lo = it->second;
+    *hi = it->second + 1024;
+    return OCS_OK;
+}
+
+// Windows 2^16 .. 2^22: the two-launch four-step FFT over frames [f0, f1),
+// with a stream-ordered scratch area of at most ~1 GB (frames in chunks).
+int launch_large_frames(const Request& r, const float* d_sig, uint64_t n, float* d_out, uint64_t f0, uint64_t f1,
+                        cudaStream_t st)
+{
+    if (f1 <= f0) return OCS_OK;
+    const int e1 = ocs::large_m1_log2(r.exp) + 1, e2 = ocs::large_m2_log2(r.exp) + 1;
+    ocs::LargeArgs a{};
+    int rc = get_twiddles(e1, false, &a.tw1);
+    if (!rc) rc = get_twiddles(e2, false, &a.tw2);
+    if (!rc) rc = get_window(r.opt.window, r.exp, r.opt.sigma, true, &a.win);
+    const uint64_t N = r.geo.n_window, M = N / 2;
+    if (!rc) rc = get_two_level(M, &a.twm_lo, &a.twm_hi);
+    if (!rc) rc = get_two_level(N, &a.twn_lo, &a.twn_hi);
+    if (rc) return rc;
+    a.x = d_sig;
+    a.n = n;
+    a.hop = r.geo.hop;
+    a.frames_total = f1;
+    a.out = d_out;
+    a.ohalf = r.opt.half_complex && !r.opt.dense ? (uint64_t)r.geo.ohalf : 0;
+    a.dense = r.opt.dense;
+    a.remove_dc = r.opt.remove_dc;
+    a.m1 = 1ull << (e1 - 1);
+    a.m2 = 1ull << (e2 - 1);
+    const int outk = r.opt.half_complex ? ocs::OUT_HALF : (r.opt.serial_power ? ocs::OUT_POWER_SERIAL : ocs::OUT_POWER);
+    // scratch per chunk (OCS_LARGE_SCRATCH_MB overrides).  Measured on GB300
+    // at 1e8 samples: chunks small enough for the scratch to stay in L2
+    // (16-96 MB) lose to fewer, fuller launch pairs; 1 GB is the default
+    uint64_t scratch_bytes = 1024ull << 20;
+    if (const char* sb = std::getenv("OCS_LARGE_SCRATCH_MB")) scratch_bytes = std::max(1L, std::atol(sb)) << 20;
+    const uint64_t per = std::max<uint64_t>(1, std::min<uint64_t>(f1 - f0, scratch_bytes / (M * sizeof(float2))));
+    float2* scratch = nullptr;
+    OCS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&scratch), per * M * sizeof(float2), st));
+    a.scratch = scratch;
+    cudaError_t e = cudaSuccess;
+    for (uint64_t c0 = f0; c0 < f1 && e == cudaSuccess; c0 += per) {
+        a.f0 = c0;
+        e = ocs::launch_large(r.exp, outk, a, std::min(per, f1 - c0), st);
+    }
+    const cudaError_t e2b = cudaFreeAsync(scratch, st);
+    if (e != cudaSuccess) return cuda_fail(e, "large-window launch");
+    if (e2b != cudaSuccess) return cuda_fail(e2b, "large-window scratch");
+    return OCS_OK;
+}
+
 // Launch the fused kernel for frames [f0, f1) of a request.  The first launch
 // of a new (window, output kind, layout, size class) measures every kernel
 // variant that applies on the request's own buffers and keeps the fastest
@@ -317,6 +383,7 @@ int ilog2u(uint64_t v)
 int launch_frames(const Request& r, const float* d_sig, uint64_t n, float* d_out, uint64_t f0, uint64_t f1,
                   cudaStream_t st)
 {
+    if (ocs::large_supports(r.exp)) return launch_large_frames(r, d_sig, n, d_out, f0, f1, st);
     const float2* tw_single = nullptr;
     const float2* tw_pair = nullptr;
     const float* win = nullptr;
@@ -747,8 +814,10 @@ void ocs_shutdown(void)
     cudaDeviceSynchronize();
     for (auto& kv : c.twiddles) cudaFree(kv.second);
     for (auto& kv : c.windows) cudaFree(kv.second);
+    for (auto& kv : c.two_level) cudaFree(kv.second);
     c.twiddles.clear();
     c.windows.clear();
+    c.two_level.clear();
     for (Slot* s : c.all_slots) {
         cudaStreamDestroy(s->s_h2d);
         cudaStreamDestroy(s->s_comp);

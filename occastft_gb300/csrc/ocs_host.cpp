@@ -58,7 +58,7 @@ std::string parse_options(const char* options, Options& o)
 std::string make_geometry(uint64_t n, int exp, float overlap, const Options& o, Geometry& g)
 {
     if (exp < 6) return "Operation not supported";
-    if (exp > 15) return "Operation not supported: window sizes above 2^15";
+    if (exp > 22) return "Operation not supported: window sizes above 2^22";
     if (n == 0) return "empty input signal";
     if (n > 0xffffffffull) return "signal longer than 2^32-1 samples";
     if (!(overlap < 1.0f) || std::isnan(overlap)) return "overlap ratio must be below 1";

@@ -63,6 +63,35 @@ size_t batch_smem_bytes();
 cudaError_t launch_batch(const FusedArgs* d_reqs, const BatchTile* d_tiles, const uint32_t* d_ntiles,
                          uint32_t* d_counter, int grid, cudaStream_t st);
 
+// windows 2^16 .. 2^22: four-step FFT in two launches (column pass, row pass)
+constexpr int kLargeMinExp = 16;
+constexpr int kLargeMaxExp = 22;
+struct LargeArgs {
+    const float* x;          // whole signal
+    uint64_t n;              // its samples
+    uint64_t hop;
+    uint64_t f0;             // first frame of this launch (absolute)
+    uint64_t frames_total;   // frames below this index are computed
+    const float* win;        // window table scaled by 1/2 (N floats)
+    float2* scratch;         // frames of this launch x M complex
+    float* out;              // whole output
+    uint64_t ohalf;          // compat half-complex: complex outputs in total
+    int dense;
+    int remove_dc;
+    uint64_t m1, m2;         // M = m1 * m2 complex points per frame
+    const float2* tw1;       // Stockham table of the m1-point FFT (plan of window 2 m1)
+    const float2* tw2;       // Stockham table of the m2-point FFT (plan of window 2 m2)
+    const float2* twm_lo;    // exp(-2 pi i j / M): lo[j % 1024] * hi[j / 1024]
+    const float2* twm_hi;
+    const float2* twn_lo;    // exp(-2 pi i k / N), same split
+    const float2* twn_hi;
+};
+bool large_supports(int exp);
+int large_m1_log2(int exp);
+int large_m2_log2(int exp);
+cudaError_t build_two_level(float2* lo, float2* hi, uint64_t L, cudaStream_t st);
+cudaError_t launch_large(int exp, int outk, const LargeArgs& a, uint64_t frames, cudaStream_t st);
+
 // tensor-core split-precision form (tcgen05), windows 2^8 and 2^10
 bool tc_supports(int exp);
 // err: word the kernel sets to 1 when a pipeline wait gives up (after about a

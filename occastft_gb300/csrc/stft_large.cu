@@ -1,0 +1,281 @@
+// STFT for windows 2^16 .. 2^22 (sm_103a): a four-step FFT in two launches.
+//
+// One frame of N real samples is the M = N/2 point complex FFT of
+// z[m] = y[2m] + i y[2m+1] plus the real-input untangle, as in the fused
+// kernels; here M = M1 * M2 does not fit one CTA, so with m = c + M2 m1 and
+// k = k1 + M1 k2:
+//   column pass  Y[k1][c]  = W_M^{c k1} * sum_{m1} z[c + M2 m1] W_{M1}^{m1 k1}
+//   row pass     Z[k1 + M1 k2] = sum_c Y[k1][c] W_{M2}^{c k2}
+// followed by X[k] = (Z[k] + conj Z[M-k]) + W_N^k (Z[k] - conj Z[M-k]) / i and
+// X[k + M] = (Z[k] + conj Z[M-k]) - W_N^k (...) (the window table carries the
+// untangle's factor 1/2).
+//
+// Column pass: a CTA owns 8 consecutive columns of one frame.  It reads the
+// frame's samples row by row (64 contiguous bytes per row), applies the
+// window, runs 8 M1-point FFTs with the fused kernels' Stockham core, applies
+// W_M^{c k1} and writes Y row-major to a scratch area (again 64-byte rows).
+// Row pass: a CTA owns 8 rows k1 and their 8 mirror rows M1 - k1 (row M1/2
+// stands in for the mirror of row 0), so every Z[M-k] it needs is its own.
+// It runs 16 M2-point FFTs, then writes outputs with lanes over k1, i.e. 8
+// consecutive bins per (k2) run.
+//
+// DC removal subtracts the mean of the windowed frame; in the transform that
+// changes bin 0 only (to zero), which is what the row pass writes.  The
+// reference's EXPC runs any exponent >= 12 through a radix-2 Stockham
+// (RunnerCommon.cpp:278-289, Serial/src/functionImpl.cpp:186-270).
+#include "stft_fused_kernel.cuh"
+
+namespace ocs {
+namespace {
+
+constexpr int kTileC = 8;  // columns per column-pass CTA
+constexpr int kTileR = 8;  // rows (and as many mirror rows) per row-pass CTA
+
+__host__ __device__ constexpr int large_l1(int exp) { return exp / 2; }         // log2 M1
+__host__ __device__ constexpr int large_l2(int exp) { return exp - 1 - exp / 2; }  // log2 M2
+
+// exp(-2 pi i j / L) from a two-level table: lo[j & 1023] * hi[j >> 10]
+__device__ __forceinline__ float2 tw2l(const float2* lo, const float2* hi, uint64_t j)
+{
+    return cmul(lo[j & 1023u], hi[j >> 10]);
+}
+
+// ---------------------------------------------------------------- column pass
+template <int EXP1>
+__global__ void __launch_bounds__(kTileC * (fused_M(EXP1) / fused_cfg(EXP1).R))
+    large_columns_kernel(const LargeArgs a)
+{
+    using K = Core<EXP1>;
+    constexpr int M1 = K::M, R = K::R, T = K::T;
+    constexpr int BS = fused_buf_stride(EXP1);
+    extern __shared__ float2 sbuf[];  // kTileC column buffers of BS slots
+    const int tid = threadIdx.x;
+    const uint64_t M2 = a.m2;
+    const uint64_t tiles = M2 / kTileC;
+    const uint64_t fl = blockIdx.x / tiles;  // frame within this launch
+    const uint64_t c0 = (blockIdx.x % tiles) * kTileC;
+    const uint64_t f = a.f0 + fl;
+    const uint64_t s0 = f * a.hop;
+
+    // rows of 8 complex samples (16 floats, 64 bytes): lane pairs take one row
+    for (int e = tid; e < M1 * kTileC; e += blockDim.x) {
+        const int col = e % kTileC, m1 = e / kTileC;
+        const uint64_t m = c0 + col + M2 * (uint64_t)m1;  // complex index in the frame
+        const uint64_t i = 2 * m;                          // real sample index in the frame
+        const uint64_t g = s0 + i;
+        float xr = 0.0f, xi = 0.0f;
+        if (f < a.frames_total) {
+            if (g < a.n) xr = a.x[g];
+            if (g + 1 < a.n) xi = a.x[g + 1];
+        }
+        const float2 w = *reinterpret_cast<const float2*>(a.win + i);
+        sbuf[col * BS + K::pd(m1)] = make_float2(xr * w.x, xi * w.y);
+    }
+    __syncthreads();
+    const int col = tid / T, t = tid % T;
+    float2* buf = sbuf + col * BS;
+    float2 v[R];
+#pragma unroll
+    for (int u = 0; u < R; ++u) v[u] = buf[K::pd(t + u * T)];
+    K::fft(v, buf, a.tw1, t);  // slot u holds column FFT bin k1 = t + u*T
+    __syncthreads();
+    const uint64_t c = c0 + col;
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+        const int k1 = t + u * T;
+        buf[K::pd(k1)] = cmul(v[u], tw2l(a.twm_lo, a.twm_hi, c * (uint64_t)k1));
+    }
+    __syncthreads();
+    float2* y = a.scratch + fl * (uint64_t)M1 * M2;
+    for (int e = tid; e < M1 * kTileC; e += blockDim.x) {
+        const int cc = e % kTileC, k1 = e / kTileC;
+        y[(uint64_t)k1 * M2 + c0 + cc] = sbuf[cc * BS + K::pd(k1)];
+    }
+}
+
+// ---------------------------------------------------------------- row pass
+template <int EXP2, int OUTK>
+__global__ void __launch_bounds__(2 * kTileR * (fused_M(EXP2) / fused_cfg(EXP2).R))
+    large_rows_kernel(const LargeArgs a)
+{
+    using K = Core<EXP2>;
+    constexpr int M2 = K::M, R = K::R, T = K::T;
+    constexpr int BS = fused_buf_stride(EXP2);
+    extern __shared__ float2 sbuf[];  // 2*kTileR row buffers of BS slots
+    const int tid = threadIdx.x;
+    const uint64_t M1 = a.m1;
+    const uint64_t M = M1 * M2;
+    const uint64_t N = 2 * M;
+    const uint64_t blocks = M1 / (2 * kTileR);
+    const uint64_t fl = blockIdx.x / blocks;
+    const uint64_t b = blockIdx.x % blocks;
+    const uint64_t f = a.f0 + fl;
+
+    // slot s < kTileR: row b*8 + s; slot kTileR + s: its mirror M1 - row,
+    // except that row 0's mirror slot holds row M1/2
+    auto row_of = [&](int s) -> uint64_t {
+        const uint64_t d = b * kTileR + (uint64_t)(s % kTileR);
+        if (s < kTileR) return d;
+        return d == 0 ? M1 / 2 : M1 - d;
+    };
+    const int rs = tid / T, t = tid % T;
+    const float2* y = a.scratch + fl * M;
+    float2* buf = sbuf + rs * BS;
+    {
+        const float2* yr = y + row_of(rs) * M2;
+        float2 v[R];
+#pragma unroll
+        for (int u = 0; u < R; ++u) v[u] = yr[t + u * T];
+        K::fft(v, buf, a.tw2, t);  // slot u: Z[k1 + M1 (t + u T)]
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < R; ++u) buf[K::pd(t + u * T)] = v[u];
+    }
+    __syncthreads();
+    if (f >= a.frames_total) return;
+
+    // outputs: lanes over the 8 rows of a slot group, then over k2
+    const bool dc = a.remove_dc != 0;
+    for (int e = tid; e < 2 * kTileR * M2; e += blockDim.x) {
+        const int s = (e % kTileR) + kTileR * (e / (kTileR * M2));
+        const int k2 = (e / kTileR) % M2;
+        const uint64_t k1 = row_of(s);
+        // partner Z[M - k]: row (M1 - k1) mod M1; column M2-1-k2, or (M2-k2) mod M2 for row 0
+        int ps, pk2;
+        if (k1 == 0) {
+            ps = s;
+            pk2 = (M2 - k2) & (M2 - 1);
+        } else if (k1 == M1 / 2) {
+            ps = s;
+            pk2 = M2 - 1 - k2;
+        } else {
+            ps = s < kTileR ? s + kTileR : s - kTileR;
+            pk2 = M2 - 1 - k2;
+        }
+        const float2 A = sbuf[s * BS + K::pd(k2)];
+        const float2 B = sbuf[ps * BS + K::pd(pk2)];
+        const uint64_t k = k1 + M1 * (uint64_t)k2;
+        float2 ev, wo;
+        K::untangle(A, B, tw2l(a.twn_lo, a.twn_hi, k), ev, wo);
+        float2 X0 = make_float2(ev.x + wo.x, ev.y + wo.y);        // X[k]
+        const float2 X1 = make_float2(ev.x - wo.x, ev.y - wo.y);  // X[k + M]
+        if (dc && k == 0) X0 = make_float2(0.0f, 0.0f);
+        if constexpr (OUTK == OUT_HALF) {
+            float2* o2 = reinterpret_cast<float2*>(a.out);
+            if (!a.dense) {
+                const uint64_t flat = f * N + k;
+                if (flat < a.ohalf) __stcs(o2 + flat, X0);
+                if (flat + M < a.ohalf) __stcs(o2 + flat + M, X1);
+            } else {
+                float2* ro = o2 + f * (M + 1);
+                __stcs(ro + k, X0);
+                if (k == 0) __stcs(ro + M, X1);
+            }
+        } else {
+            const float p0 = power_of<OUTK>(X0), p1 = power_of<OUTK>(X1);
+            if (!a.dense) {
+                float* ro = a.out + f * N;
+                __stcs(ro + k, p0);
+                __stcs(ro + k + M, p1);
+            } else {
+                float* ro = a.out + f * (M + 1);
+                __stcs(ro + k, p0);
+                if (k == 0) __stcs(ro + M, p1);
+            }
+        }
+    }
+}
+
+__global__ void build_two_level_kernel(float2* lo, float2* hi, uint64_t L, uint64_t nhi)
+{
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < 1024 + nhi;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t j = i < 1024 ? i : (i - 1024) * 1024;
+        double s, c;
+        sincospi(-2.0 * (double)(j % L) / (double)L, &s, &c);
+        const float2 w = make_float2((float)c, (float)s);
+        if (i < 1024) lo[i] = w;
+        else hi[i - 1024] = w;
+    }
+}
+
+template <int EXP1>
+cudaError_t launch_columns_t(const LargeArgs& a, uint64_t frames, cudaStream_t st)
+{
+    constexpr int T = fused_M(EXP1) / fused_cfg(EXP1).R;
+    constexpr size_t smem = (size_t)kTileC * fused_buf_stride(EXP1) * sizeof(float2);
+    auto k = large_columns_kernel<EXP1>;
+    static bool attr = false;
+    if (!attr) {
+        const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const uint64_t grid = frames * (a.m2 / kTileC);
+    k<<<(unsigned)grid, kTileC * T, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int EXP2, int OUTK>
+cudaError_t launch_rows_t(const LargeArgs& a, uint64_t frames, cudaStream_t st)
+{
+    constexpr int T = fused_M(EXP2) / fused_cfg(EXP2).R;
+    constexpr size_t smem = (size_t)2 * kTileR * fused_buf_stride(EXP2) * sizeof(float2);
+    auto k = large_rows_kernel<EXP2, OUTK>;
+    static bool attr = false;
+    if (!attr) {
+        const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const uint64_t grid = frames * (a.m1 / (2 * kTileR));
+    k<<<(unsigned)grid, 2 * kTileR * T, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <int EXP2>
+cudaError_t launch_rows_e(int outk, const LargeArgs& a, uint64_t frames, cudaStream_t st)
+{
+    switch (outk) {
+    case OUT_POWER: return launch_rows_t<EXP2, OUT_POWER>(a, frames, st);
+    case OUT_POWER_SERIAL: return launch_rows_t<EXP2, OUT_POWER_SERIAL>(a, frames, st);
+    case OUT_HALF: return launch_rows_t<EXP2, OUT_HALF>(a, frames, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace
+
+bool large_supports(int exp) { return exp >= kLargeMinExp && exp <= kLargeMaxExp; }
+int large_m1_log2(int exp) { return large_l1(exp); }
+int large_m2_log2(int exp) { return large_l2(exp); }
+
+cudaError_t build_two_level(float2* lo, float2* hi, uint64_t L, cudaStream_t st)
+{
+    const uint64_t nhi = (L + 1023) / 1024;
+    build_two_level_kernel<<<64, 256, 0, st>>>(lo, hi, L, nhi);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_large(int exp, int outk, const LargeArgs& a, uint64_t frames, cudaStream_t st)
+{
+    if (!large_supports(exp) || frames == 0) return cudaErrorInvalidValue;
+    cudaError_t e;
+    switch (large_l1(exp) + 1) {  // EXP1: the M1-point FFT is the core of window 2^EXP1
+    case 9: e = launch_columns_t<9>(a, frames, st); break;
+    case 10: e = launch_columns_t<10>(a, frames, st); break;
+    case 11: e = launch_columns_t<11>(a, frames, st); break;
+    case 12: e = launch_columns_t<12>(a, frames, st); break;
+    default: return cudaErrorInvalidValue;
+    }
+    if (e != cudaSuccess) return e;
+    switch (large_l2(exp) + 1) {
+    case 8: return launch_rows_e<8>(outk, a, frames, st);
+    case 9: return launch_rows_e<9>(outk, a, frames, st);
+    case 10: return launch_rows_e<10>(outk, a, frames, st);
+    case 11: return launch_rows_e<11>(outk, a, frames, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace ocs

@@ -110,3 +110,12 @@ def test_gaussian_sigma_quirk(ocs_lib, orc):
     # "--gaussian_window=4.312345<<sigma": the first sigma character is skipped
     rc, o, _ = orc.parse_options("--gaussian_window=4.312345<<sigma")
     assert rc == 0 and abs(o.sigma - 0.312345) < 1e-7
+
+
+def test_window_exponent_limits(ocs_lib):
+    """Windows up to 2^22 are accepted (the reference's EXPC has no upper
+    bound short of OFullSize < 2^32); 2^23 is refused with a status."""
+    g = ocs_lib.geometry(50_000_000, 22, 0.5, "--hanning_window")
+    assert g.n_window == 1 << 22 and g.out_floats == g.qt * (1 << 22)
+    with pytest.raises(ocs_lib.OcsError, match="above 2\\^22"):
+        ocs_lib.geometry(50_000_000, 23, 0.5, "")
