@@ -284,8 +284,10 @@ int prepare(uint64_t n, int exp, float ov, const char* options, Request& r)
     if (st != "OK") return fail(OCS_EPIPELINE, st);
     st = ocs::make_geometry(n, exp, ov, r.opt, r.geo);
     if (st != "OK") return fail(OCS_EINVAL, st);
-    if (r.opt.precision == 1 && !ocs::tc_supports(exp))
+    if (r.opt.precision >= 1 && !ocs::tc_supports(exp))
         return fail(OCS_EINVAL, "the tensor-core form supports windows 2^8 and 2^10");
+    if (r.opt.precision >= 2 && !ocs::tc_piped(exp, r.geo.hop))
+        return fail(OCS_EINVAL, "the bf16 tensor-core forms need a frame advance of at most the window");
     r.exp = exp;
     return OCS_OK;
 }
@@ -429,14 +431,14 @@ int launch_frames(const Request& r, const float* d_sig, uint64_t n, float* d_out
     a.cs = ((hop % 4 == 0) && (xa & 15u) == 0) ? 16 : (a.vec2 ? 8 : 4);
     const bool out16 = (reinterpret_cast<uintptr_t>(a.out) & 15u) == 0;
 
-    if (r.opt.precision == 1) {
+    if (r.opt.precision >= 1) {
         // tensor-core form: unscaled window (no real-input untangle)
         const float* w1 = nullptr;
         rc = get_window(r.opt.window, r.exp, r.opt.sigma, false, &w1);
         if (rc) return rc;
         a.win = w1;
         Context& c = ctx();
-        OCS_CUDA(ocs::launch_tc(r.exp, outk, a, c.d_err, c.tc_test_stall, c.sms, st));
+        OCS_CUDA(ocs::launch_tc(r.exp, outk, r.opt.precision, a, c.d_err, c.tc_test_stall, c.sms, st));
         return OCS_OK;
     }
 
@@ -872,7 +874,7 @@ int ocs_activate_device(const float* d_in, uint64_t n, int exp, float ov, const 
     rc = ensure_init();
     if (rc) return rc;
     // asynchronous: a timed-out earlier tensor-core launch is reported here
-    if (r.opt.precision == 1) {
+    if (r.opt.precision >= 1) {
         rc = take_tc_error();
         if (rc) return rc;
     }
@@ -962,7 +964,7 @@ int ocs_activate(const float* in, uint64_t n, int exp, float ov, const char* opt
     if (e != cudaSuccess) return cuda_fail(e, "ocs_activate");
     if (e2 != cudaSuccess) return cuda_fail(e2, "ocs_activate sync");
     if (e3 != cudaSuccess) return cuda_fail(e3, "ocs_activate sync");
-    if (r.opt.precision == 1) {
+    if (r.opt.precision >= 1) {
         rc = take_tc_error();
         if (rc) return rc;
     }

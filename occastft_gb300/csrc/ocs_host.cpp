@@ -52,6 +52,8 @@ std::string parse_options(const char* options, Options& o)
     o.dense = s.find("--layout=dense") != std::string::npos;
     o.serial_power = s.find("--serial_power") != std::string::npos;
     if (s.find("--precision=tc-fp16") != std::string::npos) o.precision = 1;
+    if (s.find("--precision=tc-bf16x2") != std::string::npos) o.precision = 2;
+    if (s.find("--precision=tc-bf16x3") != std::string::npos) o.precision = 3;
     return "OK";
 }
 

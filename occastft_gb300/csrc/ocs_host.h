@@ -26,7 +26,9 @@ struct Options {
     bool half_complex = false;
     bool dense = false;
     bool serial_power = false;
-    int precision = 0;  // 0 plain FP32; 1 tensor cores, fp16 hi/lo split (--precision=tc-fp16)
+    // 0 plain FP32; tensor cores with split operands: 1 fp16 hi/lo
+    // (--precision=tc-fp16), 2 bf16 hi/lo (tc-bf16x2), 3 bf16 hi/mid/lo (tc-bf16x3)
+    int precision = 0;
 };
 
 struct Geometry {

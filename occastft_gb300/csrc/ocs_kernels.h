@@ -97,7 +97,12 @@ bool tc_supports(int exp);
 // err: word the kernel sets to 1 when a pipeline wait gives up (after about a
 // second); test_stall: test hook, the first input phase of each CTA never
 // completes so that every wait runs out
-cudaError_t launch_tc(int exp, int outk, const FusedArgs& a, int* err, int test_stall, int sms, cudaStream_t st);
+// pm: operand split, 1 fp16 hi/lo, 2 bf16 hi/lo, 3 bf16 hi/mid/lo.  The
+// pipelined kernel needs hop <= N (tc_piped); longer frame advances take the
+// first, fp16-only kernel.
+bool tc_piped(int exp, uint64_t hop);
+cudaError_t launch_tc(int exp, int outk, int pm, const FusedArgs& a, int* err, int test_stall, int sms,
+                      cudaStream_t st);
 
 // unfused per-stage kernels behind the runnerFunction hooks
 cudaError_t launch_overlap(const float* in, uint32_t ofull, uint32_t n, uint32_t exp, uint32_t hop,

@@ -23,6 +23,7 @@
 // frees its tensor memory and returns.
 #include "ocs_kernels.h"
 
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
 #include <cstdint>
@@ -498,38 +499,90 @@ __device__ __forceinline__ bool mbar_wait_t(uint64_t* mbar, uint32_t parity, con
     return false;
 }
 
-// fp16 hi/lo split with packed conversions (two values per instruction)
-__device__ __forceinline__ void split8p(const float (&x)[8], uint4& hi, uint4& lo)
-{
-    uint32_t h[4], l[4];
+// Operand splits.  PM_FP16X2: x = hi + lo in fp16 (products hh + hl + lh);
+// PM_BF16X2: the same in bf16 (8-bit significands: about 16 bits kept, for
+// reference); PM_BF16X3: x = hi + mid + lo in bf16 (products hh, hm, mh, hl,
+// lh, mm: about 24 bits, fp32-like).  Packed conversions, two values each.
+enum { PM_FP16X2 = 1, PM_BF16X2 = 2, PM_BF16X3 = 3 };
+template <int PM>
+struct Split {
+    static constexpr int PARTS = PM == PM_BF16X3 ? 3 : 2;
+    static constexpr uint32_t FMT = PM == PM_FP16X2 ? 0u : 1u;  // tcgen05 kind::f16 operand format
+    // p[k] receives part k of x[0..7], 8 halves in 16 bytes
+    static __device__ __forceinline__ void split8(const float (&x)[8], uint4 (&p)[PARTS])
+    {
+        uint32_t w[PARTS][4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const __half2 a = __floats2half2_rn(x[2 * i], x[2 * i + 1]);
-        const float2 b = __half22float2(a);
-        const __half2 c = __floats2half2_rn(x[2 * i] - b.x, x[2 * i + 1] - b.y);
-        h[i] = *reinterpret_cast<const uint32_t*>(&a);
-        l[i] = *reinterpret_cast<const uint32_t*>(&c);
+        for (int i = 0; i < 4; ++i) {
+            float a = x[2 * i], b = x[2 * i + 1];
+#pragma unroll
+            for (int k = 0; k < PARTS; ++k) {
+                if constexpr (PM == PM_FP16X2) {
+                    const __half2 h = __floats2half2_rn(a, b);
+                    const float2 f = __half22float2(h);
+                    w[k][i] = *reinterpret_cast<const uint32_t*>(&h);
+                    a -= f.x;
+                    b -= f.y;
+                } else {
+                    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+                    const float2 f = __bfloat1622float2(h);
+                    w[k][i] = *reinterpret_cast<const uint32_t*>(&h);
+                    a -= f.x;
+                    b -= f.y;
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < PARTS; ++k) p[k] = make_uint4(w[k][0], w[k][1], w[k][2], w[k][3]);
     }
-    hi = make_uint4(h[0], h[1], h[2], h[3]);
-    lo = make_uint4(l[0], l[1], l[2], l[3]);
+    static __device__ __forceinline__ void part1(float v, uint16_t (&o)[PARTS])
+    {
+#pragma unroll
+        for (int k = 0; k < PARTS; ++k) {
+            if constexpr (PM == PM_FP16X2) {
+                const __half h = __float2half_rn(v);
+                o[k] = __half_as_ushort(h);
+                v -= __half2float(h);
+            } else {
+                const __nv_bfloat16 h = __float2bfloat16_rn(v);
+                o[k] = __bfloat16_as_ushort(h);
+                v -= __bfloat162float(h);
+            }
+        }
+    }
+};
+
+// instruction descriptor of kind::f16 with the mode's operand format
+template <int PM>
+__host__ __device__ constexpr uint32_t idesc_pm(int M, int N)
+{
+    return idesc_f16(M, N) | (Split<PM>::FMT << 7) | (Split<PM>::FMT << 10);
 }
 
-template <int R>
+template <int R, int PM>
 struct Tc2Cfg {
+    static constexpr int P = Split<PM>::PARTS;
     static constexpr int N = R * R;
     static constexpr int FPT = 128 / R;
     static constexpr int K1 = R, K2 = 2 * R, NO = 2 * R;
     static constexpr uint32_t RAW_BYTES = ((FPT * N + 64) * 4 + 1023) / 1024 * 1024;  // span of hop <= N
-    static constexpr uint32_t A1_BYTES = 2 * (K1 / 8) * 2048;
-    static constexpr uint32_t A2_BYTES = 2 * (K2 / 8) * 2048;
-    static constexpr uint32_t B1_BYTES = 2 * NO * 128;
-    static constexpr uint32_t B2_BYTES = 2 * NO * 128;
+    static constexpr uint32_t A1_PART = (K1 / 8) * 2048;  // 128 rows, MN-major
+    static constexpr uint32_t A2_PART = (K2 / 8) * 2048;
+    static constexpr uint32_t A1_BYTES = P * A1_PART;
+    static constexpr uint32_t A2_BYTES = P * A2_PART;
+    static constexpr uint32_t B_PART = NO * 128;  // K <= 64: one 128-byte row per output column
+    static constexpr uint32_t B1_BYTES = P * B_PART;
+    static constexpr uint32_t B2_BYTES = P * B_PART;
     static constexpr uint32_t TW_BYTES = N * 8;
     static constexpr uint32_t TAB_BYTES = B1_BYTES + B2_BYTES + TW_BYTES;  // the prebuilt image
+    // A2 double-buffered unless that overflows shared memory (bf16x3 at R = 32)
+    static constexpr int NA2 = (2 * RAW_BYTES + 2 * A1_BYTES + 2 * A2_BYTES + TAB_BYTES + N * 4 + 2048) <= 227 * 1024
+                                   ? 2
+                                   : 1;
     static constexpr uint32_t OFF_RAW = 0;
     static constexpr uint32_t OFF_A1 = OFF_RAW + 2 * RAW_BYTES;
     static constexpr uint32_t OFF_A2 = OFF_A1 + 2 * A1_BYTES;
-    static constexpr uint32_t OFF_B1 = OFF_A2 + 2 * A2_BYTES;
+    static constexpr uint32_t OFF_B1 = OFF_A2 + NA2 * A2_BYTES;
     static constexpr uint32_t OFF_B2 = OFF_B1 + B1_BYTES;
     static constexpr uint32_t OFF_TW = OFF_B2 + B2_BYTES;
     static constexpr uint32_t OFF_WIN = OFF_TW + TW_BYTES;
@@ -538,18 +591,25 @@ struct Tc2Cfg {
     static constexpr uint32_t SMEM = OFF_MISC + 512 + 1024;
     static constexpr uint32_t TMEM_COLS = 4 * NO <= 128 ? 128 : 256;
     static_assert(TAB_BYTES % 16 == 0, "table image copied in 16-byte units");
+    static_assert(SMEM <= 227 * 1024, "shared memory");
 };
 
-__device__ __align__(1024) unsigned char g_tc_tab16[Tc2Cfg<16>::TAB_BYTES];
-__device__ __align__(1024) unsigned char g_tc_tab32[Tc2Cfg<32>::TAB_BYTES];
+// prebuilt table images, one per window size and split mode
+__device__ __align__(1024) unsigned char g_tc_tab16_1[Tc2Cfg<16, 1>::TAB_BYTES];
+__device__ __align__(1024) unsigned char g_tc_tab16_2[Tc2Cfg<16, 2>::TAB_BYTES];
+__device__ __align__(1024) unsigned char g_tc_tab16_3[Tc2Cfg<16, 3>::TAB_BYTES];
+__device__ __align__(1024) unsigned char g_tc_tab32_1[Tc2Cfg<32, 1>::TAB_BYTES];
+__device__ __align__(1024) unsigned char g_tc_tab32_2[Tc2Cfg<32, 2>::TAB_BYTES];
+__device__ __align__(1024) unsigned char g_tc_tab32_3[Tc2Cfg<32, 3>::TAB_BYTES];
 
 // B1: rows 2k1 (re), 2k1+1 (im) of the real-input r-point DFT, K = m.
 // B2: the complex r-point DFT as a real matrix, K = g (re part, k < R) and
 // g (im part, k >= R).  TW: W_N^{g k1} / R, stored [k1][g].
-template <int R>
+template <int R, int PM>
 __global__ void build_tc_tables_kernel(unsigned char* img)
 {
-    using C = Tc2Cfg<R>;
+    using C = Tc2Cfg<R, PM>;
+    using S = Split<PM>;
     unsigned char* B1 = img;
     unsigned char* B2 = img + C::B1_BYTES;
     float2* TW = reinterpret_cast<float2*>(img + C::B1_BYTES + C::B2_BYTES);
@@ -558,10 +618,9 @@ __global__ void build_tc_tables_kernel(unsigned char* img)
         const int row = e / C::K1, m = e % C::K1, k1 = row >> 1;
         double sn, cs;
         sincospi(2.0 * (double)((m * k1) % R) / (double)R, &sn, &cs);
-        const float w = (row & 1) ? (float)(-sn) : (float)cs;
-        const __half h = __float2half_rn(w), l = __float2half_rn(w - __half2float(h));
-        *reinterpret_cast<__half*>(B1 + k_off(row, m)) = h;
-        *reinterpret_cast<__half*>(B1 + C::B1_BYTES / 2 + k_off(row, m)) = l;
+        uint16_t pt[S::PARTS];
+        S::part1((row & 1) ? (float)(-sn) : (float)cs, pt);
+        for (int k = 0; k < S::PARTS; ++k) *reinterpret_cast<uint16_t*>(B1 + k * C::B_PART + k_off(row, m)) = pt[k];
     }
     for (int e = tid; e < C::NO * C::K2; e += nth) {
         const int row = e / C::K2, k = e % C::K2, k2 = row >> 1, g = k % R;
@@ -571,9 +630,9 @@ __global__ void build_tc_tables_kernel(unsigned char* img)
         float w;
         if ((row & 1) == 0) w = (k < R) ? (float)cs : (float)sn;
         else w = (k < R) ? (float)(-sn) : (float)cs;
-        const __half h = __float2half_rn(w), l = __float2half_rn(w - __half2float(h));
-        *reinterpret_cast<__half*>(B2 + k_off(row, k)) = h;
-        *reinterpret_cast<__half*>(B2 + C::B2_BYTES / 2 + k_off(row, k)) = l;
+        uint16_t pt[S::PARTS];
+        S::part1(w, pt);
+        for (int q = 0; q < S::PARTS; ++q) *reinterpret_cast<uint16_t*>(B2 + q * C::B_PART + k_off(row, k)) = pt[q];
     }
     for (int e = tid; e < C::N; e += nth) {
         const int k1 = e / R, g = e % R;
@@ -589,11 +648,13 @@ enum { B_RAW_FULL = 0, B_RAW_EMPTY = 2, B_A1_FULL = 4, B_A1_EMPTY = 6, B_D1_FULL
 
 constexpr int kTc2Threads = 448;
 
-template <int R, int OUTK>
+template <int R, int OUTK, int PM>
 __global__ void __launch_bounds__(kTc2Threads, 1)
     stft_tc2_kernel(const FusedArgs a, const unsigned char* __restrict__ tab, volatile int* err, int test_stall)
 {
-    using C = Tc2Cfg<R>;
+    using C = Tc2Cfg<R, PM>;
+    using S = Split<PM>;
+    constexpr int P = C::P;
     constexpr int N = C::N, FPT = C::FPT;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* sm = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -657,7 +718,11 @@ __global__ void __launch_bounds__(kTc2Threads, 1)
     __syncthreads();
     fence_after();
     const uint32_t tmem = *tmem_slot;
-    constexpr uint32_t ID = idesc_f16(128, C::NO);
+    constexpr uint32_t ID = idesc_pm<PM>(128, C::NO);
+    // products kept, as (A part, B part): hi*hi first, then the cross terms
+    constexpr int NPROD = P == 3 ? 6 : 3;
+    constexpr int PA[6] = {0, 0, 1, 0, 2, 1};
+    constexpr int PB[6] = {0, 1, 0, 2, 0, 1};
 
     const uint64_t ntiles = (a.frames + FPT - 1) / FPT;
     const uint64_t cnt = blockIdx.x < ntiles ? (ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
@@ -728,13 +793,12 @@ __global__ void __launch_bounds__(kTc2Threads, 1)
                     const uint32_t d1 = tmem + s * C::NO;
 #pragma unroll
                     for (int ks = 0; ks < C::K1 / 16; ++ks) {
-                        const uint64_t ah = sdesc(a1 + ks * 4096, 1024, 2048);
-                        const uint64_t al = sdesc(a1 + C::A1_BYTES / 2 + ks * 4096, 1024, 2048);
-                        const uint64_t bh = sdesc(b1 + ks * 32, 16, 1024);
-                        const uint64_t bl = sdesc(b1 + C::B1_BYTES / 2 + ks * 32, 16, 1024);
-                        mma_f16(d1, ah, bh, ID, ks > 0);
-                        mma_f16(d1, ah, bl, ID, 1);
-                        mma_f16(d1, al, bh, ID, 1);
+#pragma unroll
+                        for (int q = 0; q < NPROD; ++q) {
+                            const uint64_t ad = sdesc(a1 + PA[q] * C::A1_PART + ks * 4096, 1024, 2048);
+                            const uint64_t bd = sdesc(b1 + PB[q] * C::B_PART + ks * 32, 16, 1024);
+                            mma_f16(d1, ad, bd, ID, (ks > 0 || q > 0) ? 1u : 0u);
+                        }
                     }
                     mma_commit(&bar[B_A1_EMPTY + s]);
                     mma_commit(&bar[B_D1_FULL + s]);
@@ -744,26 +808,27 @@ __global__ void __launch_bounds__(kTc2Threads, 1)
                     const uint64_t j = i - 1;
                     const int s = (int)(j & 1);
                     const uint32_t use = (uint32_t)(j >> 1);
-                    if (!mbar_wait_t(&bar[B_A2_FULL + s], use & 1, abort_flag) ||
+                    const int s2 = (int)(j % C::NA2);  // A2 slot
+                    const uint32_t use2 = (uint32_t)(j / C::NA2);
+                    if (!mbar_wait_t(&bar[B_A2_FULL + s2], use2 & 1, abort_flag) ||
                         (j >= 2 && !mbar_wait_t(&bar[B_D2_EMPTY + s], (use - 1) & 1, abort_flag))) {
                         give_up();
                         break;
                     }
-                    for (int q = 0; q < FPT; ++q) sD[s * FPT + q] = sC[s * FPT + q];
+                    for (int q = 0; q < FPT; ++q) sD[s * FPT + q] = sC[s2 * FPT + q];
                     fence_after();
-                    const uint32_t a2 = smem_u32(A2 + s * C::A2_BYTES);
+                    const uint32_t a2 = smem_u32(A2 + s2 * C::A2_BYTES);
                     const uint32_t d2 = tmem + 2 * C::NO + s * C::NO;
 #pragma unroll
                     for (int ks = 0; ks < C::K2 / 16; ++ks) {
-                        const uint64_t ah = sdesc(a2 + ks * 4096, 1024, 2048);
-                        const uint64_t al = sdesc(a2 + C::A2_BYTES / 2 + ks * 4096, 1024, 2048);
-                        const uint64_t bh = sdesc(b2 + ks * 32, 16, 1024);
-                        const uint64_t bl = sdesc(b2 + C::B2_BYTES / 2 + ks * 32, 16, 1024);
-                        mma_f16(d2, ah, bh, ID, ks > 0);
-                        mma_f16(d2, ah, bl, ID, 1);
-                        mma_f16(d2, al, bh, ID, 1);
+#pragma unroll
+                        for (int q = 0; q < NPROD; ++q) {
+                            const uint64_t ad = sdesc(a2 + PA[q] * C::A2_PART + ks * 4096, 1024, 2048);
+                            const uint64_t bd = sdesc(b2 + PB[q] * C::B_PART + ks * 32, 16, 1024);
+                            mma_f16(d2, ad, bd, ID, (ks > 0 || q > 0) ? 1u : 0u);
+                        }
                     }
-                    mma_commit(&bar[B_A2_EMPTY + s]);
+                    mma_commit(&bar[B_A2_EMPTY + s2]);
                     mma_commit(&bar[B_D2_FULL + s]);
                     mbar_arrive(&bar[B_D2_FULL + s]);
                 }
@@ -847,13 +912,13 @@ __global__ void __launch_bounds__(kTc2Threads, 1)
                     float v[8];
 #pragma unroll
                     for (int q = 0; q < 8; ++q) v[q] = x[8 * j + q] * sc;
-                    uint4 hi, lo;
-                    split8p(v, hi, lo);
+                    uint4 pt[P];
+                    S::split8(v, pt);
                     // samples 8c..8c+7 = (g0..g0+7, m) with g = i mod R, m = i / R
                     const int i0 = 8 * c, m = i0 / R, g0 = i0 % R;
                     const uint32_t dst = mn_off(lf * R + g0, m);
-                    *reinterpret_cast<uint4*>(a1 + dst) = hi;
-                    *reinterpret_cast<uint4*>(a1 + C::A1_BYTES / 2 + dst) = lo;
+#pragma unroll
+                    for (int k = 0; k < P; ++k) *reinterpret_cast<uint4*>(a1 + k * C::A1_PART + dst) = pt[k];
                 }
             }
             mbar_arrive(&bar[B_RAW_EMPTY + s]);
@@ -884,13 +949,15 @@ __global__ void __launch_bounds__(kTc2Threads, 1)
             }
             fence_before();
             mbar_arrive(&bar[B_D1_EMPTY + s]);
-            const bool ok2 = i < 2 || mbar_wait_t(&bar[B_A2_EMPTY + s], (use - 1) & 1, abort_flag);
+            const int s2 = (int)(i % C::NA2);  // A2 slot
+            const uint32_t use2 = (uint32_t)(i / C::NA2);
+            const bool ok2 = i < (uint64_t)C::NA2 || mbar_wait_t(&bar[B_A2_EMPTY + s2], (use2 - 1) & 1, abort_flag);
             if (!__all_sync(0xffffffffu, ok2)) {
                 give_up();
                 break;
             }
-            if (g == 0) sC[s * FPT + lf] = scale;
-            unsigned char* a2 = A2 + s * C::A2_BYTES;
+            if (g == 0) sC[s2 * FPT + lf] = scale;
+            unsigned char* a2 = A2 + s2 * C::A2_BYTES;
 #pragma unroll
             for (int k1b = 0; k1b < R; k1b += 8) {
                 float re[8], im[8];
@@ -902,18 +969,19 @@ __global__ void __launch_bounds__(kTc2Threads, 1)
                     re[q] = yr * w.x - yi * w.y;
                     im[q] = yr * w.y + yi * w.x;
                 }
-                uint4 hr, lr, hi_, li_;
-                split8p(re, hr, lr);
-                split8p(im, hi_, li_);
+                uint4 pr[P], pi[P];
+                S::split8(re, pr);
+                S::split8(im, pi);
                 const uint32_t or_ = mn_off(lf * R + k1b, g);
                 const uint32_t oi_ = mn_off(lf * R + k1b, R + g);
-                *reinterpret_cast<uint4*>(a2 + or_) = hr;
-                *reinterpret_cast<uint4*>(a2 + C::A2_BYTES / 2 + or_) = lr;
-                *reinterpret_cast<uint4*>(a2 + oi_) = hi_;
-                *reinterpret_cast<uint4*>(a2 + C::A2_BYTES / 2 + oi_) = li_;
+#pragma unroll
+                for (int k = 0; k < P; ++k) {
+                    *reinterpret_cast<uint4*>(a2 + k * C::A2_PART + or_) = pr[k];
+                    *reinterpret_cast<uint4*>(a2 + k * C::A2_PART + oi_) = pi[k];
+                }
             }
             fence_async_smem();
-            mbar_arrive(&bar[B_A2_FULL + s]);
+            mbar_arrive(&bar[B_A2_FULL + s2]);
         }
     } else {
         // ---------------- epilogue 2: row = TMEM lane = (frame, k1), holds X[k1 + R k2]
@@ -983,7 +1051,7 @@ __global__ void __launch_bounds__(kTc2Threads, 1)
     }
 }
 
-template <int R>
+template <int R, int PM>
 const unsigned char* tc_tables(cudaError_t* e)
 {
     // built once per process (one device per runner context)
@@ -992,15 +1060,19 @@ const unsigned char* tc_tables(cudaError_t* e)
     static unsigned char* img = nullptr;
     std::call_once(once, [&] {
         void* p = nullptr;
-        if constexpr (R == 16) built = cudaGetSymbolAddress(&p, g_tc_tab16);
-        else built = cudaGetSymbolAddress(&p, g_tc_tab32);
+        if constexpr (R == 16 && PM == 1) built = cudaGetSymbolAddress(&p, g_tc_tab16_1);
+        else if constexpr (R == 16 && PM == 2) built = cudaGetSymbolAddress(&p, g_tc_tab16_2);
+        else if constexpr (R == 16) built = cudaGetSymbolAddress(&p, g_tc_tab16_3);
+        else if constexpr (PM == 1) built = cudaGetSymbolAddress(&p, g_tc_tab32_1);
+        else if constexpr (PM == 2) built = cudaGetSymbolAddress(&p, g_tc_tab32_2);
+        else built = cudaGetSymbolAddress(&p, g_tc_tab32_3);
         if (built != cudaSuccess) return;
         img = static_cast<unsigned char*>(p);
         // a private stream: the caller's may be capturing a graph
         cudaStream_t s2 = nullptr;
         built = cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking);
         if (built != cudaSuccess) return;
-        build_tc_tables_kernel<R><<<8, 256, 0, s2>>>(img);
+        build_tc_tables_kernel<R, PM><<<8, 256, 0, s2>>>(img);
         built = cudaGetLastError();
         if (built == cudaSuccess) built = cudaStreamSynchronize(s2);
         cudaStreamDestroy(s2);
@@ -1009,14 +1081,14 @@ const unsigned char* tc_tables(cudaError_t* e)
     return img;
 }
 
-template <int R, int OUTK>
+template <int R, int OUTK, int PM>
 cudaError_t launch_tc2_t(const FusedArgs& a, int* err, int test_stall, int sms, cudaStream_t st)
 {
-    using C = Tc2Cfg<R>;
+    using C = Tc2Cfg<R, PM>;
     cudaError_t e = cudaSuccess;
-    const unsigned char* tab = tc_tables<R>(&e);
+    const unsigned char* tab = tc_tables<R, PM>(&e);
     if (e != cudaSuccess) return e;
-    auto k = stft_tc2_kernel<R, OUTK>;
+    auto k = stft_tc2_kernel<R, OUTK, PM>;
     static bool attr = false;
     if (!attr) {
         e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM);
@@ -1028,6 +1100,22 @@ cudaError_t launch_tc2_t(const FusedArgs& a, int* err, int test_stall, int sms, 
     const uint64_t grid = ntiles < (uint64_t)sms ? ntiles : (uint64_t)sms;
     k<<<(unsigned)(grid ? grid : 1), kTc2Threads, C::SMEM, st>>>(a, tab, err, test_stall);
     return cudaGetLastError();
+}
+
+template <int R, int PM>
+cudaError_t launch_tc2_o(int outk, const FusedArgs& a, int* err, int test_stall, int sms, cudaStream_t st)
+{
+    if (outk == OUT_HALF) return launch_tc2_t<R, OUT_HALF, PM>(a, err, test_stall, sms, st);
+    if (outk == OUT_POWER_SERIAL) return launch_tc2_t<R, OUT_POWER_SERIAL, PM>(a, err, test_stall, sms, st);
+    return launch_tc2_t<R, OUT_POWER, PM>(a, err, test_stall, sms, st);
+}
+
+template <int R>
+cudaError_t launch_tc2_p(int pm, int outk, const FusedArgs& a, int* err, int test_stall, int sms, cudaStream_t st)
+{
+    if (pm == PM_BF16X2) return launch_tc2_o<R, PM_BF16X2>(outk, a, err, test_stall, sms, st);
+    if (pm == PM_BF16X3) return launch_tc2_o<R, PM_BF16X3>(outk, a, err, test_stall, sms, st);
+    return launch_tc2_o<R, PM_FP16X2>(outk, a, err, test_stall, sms, st);
 }
 
 template <int R, int OUTK>
@@ -1052,20 +1140,17 @@ cudaError_t launch_tc_t(const FusedArgs& a, int* err, int sms, cudaStream_t st)
 
 bool tc_supports(int exp) { return exp == 8 || exp == 10; }
 
-cudaError_t launch_tc(int exp, int outk, const FusedArgs& a, int* err, int test_stall, int sms, cudaStream_t st)
+bool tc_piped(int exp, uint64_t hop) { return hop <= (1ull << exp); }
+
+cudaError_t launch_tc(int exp, int outk, int pm, const FusedArgs& a, int* err, int test_stall, int sms,
+                      cudaStream_t st)
 {
-    // the pipelined form stages one tile's input span, sized for hop <= N
-    const bool piped = a.hop <= (1ull << exp) && (reinterpret_cast<uintptr_t>(a.x) & 3u) == 0;
-    if (piped && exp == 8) {
-        if (outk == OUT_HALF) return launch_tc2_t<16, OUT_HALF>(a, err, test_stall, sms, st);
-        if (outk == OUT_POWER_SERIAL) return launch_tc2_t<16, OUT_POWER_SERIAL>(a, err, test_stall, sms, st);
-        return launch_tc2_t<16, OUT_POWER>(a, err, test_stall, sms, st);
-    }
-    if (piped && exp == 10) {
-        if (outk == OUT_HALF) return launch_tc2_t<32, OUT_HALF>(a, err, test_stall, sms, st);
-        if (outk == OUT_POWER_SERIAL) return launch_tc2_t<32, OUT_POWER_SERIAL>(a, err, test_stall, sms, st);
-        return launch_tc2_t<32, OUT_POWER>(a, err, test_stall, sms, st);
-    }
+    // the pipelined form stages one tile's input span, sized for hop <= N;
+    // the first form (fp16 split only) takes longer frame advances
+    const bool piped = tc_piped(exp, a.hop) && (reinterpret_cast<uintptr_t>(a.x) & 3u) == 0;
+    if (piped && exp == 8) return launch_tc2_p<16>(pm, outk, a, err, test_stall, sms, st);
+    if (piped && exp == 10) return launch_tc2_p<32>(pm, outk, a, err, test_stall, sms, st);
+    if (pm != PM_FP16X2) return cudaErrorInvalidValue;
     if (exp == 8) {
         if (outk == OUT_HALF) return launch_tc_t<16, OUT_HALF>(a, err, sms, st);
         if (outk == OUT_POWER_SERIAL) return launch_tc_t<16, OUT_POWER_SERIAL>(a, err, sms, st);

@@ -1,7 +1,8 @@
-"""Tensor-core split-precision form (tcgen05, --precision=tc-fp16): windows
-2^8 and 2^10, every output layout, against the FP64 oracle at the suite's
-relative-L2 bar (the form trades exact fp32 arithmetic for fp16 hi/lo
-products with fp32 accumulation)."""
+"""Tensor-core split-precision form (tcgen05): windows 2^8 and 2^10, every
+output layout, against the FP64 oracle.  fp16 hi/lo (--precision=tc-fp16) and
+bf16 hi/mid/lo (tc-bf16x3) meet the suite's relative-L2 bar of 1e-5; bf16
+hi/lo (tc-bf16x2, about 16 significant bits per operand) is reported for
+reference and held to 1e-4."""
 import numpy as np
 import pytest
 
@@ -38,6 +39,28 @@ def test_tc_scaling_extremes(ocs_lib, orc):
         got = ocs_lib.activate(x, 10, 0.75, "--hanning_window --precision=tc-fp16")
         ref = orc.fp64_stft(x, 10, 0.75, "--hanning_window")
         assert orc.rel_l2(got, ref) <= REL_L2, amp
+
+
+@pytest.mark.parametrize("prec,bar", [("tc-bf16x3", 1e-5), ("tc-bf16x2", 1e-4)])
+@pytest.mark.parametrize("exp", [8, 10])
+@pytest.mark.parametrize("opts", [
+    "--hanning_window --remove_dc",
+    "--blackman_window --half_complex_return --layout=dense",
+    "--hamming_window --half_complex_return",
+])
+def test_tc_bf16_modes(ocs_lib, orc, prec, bar, exp, opts):
+    N = 1 << exp
+    x = signal(300 + exp, 900 * N + 77)  # many tiles per CTA
+    for ov in (0.75, 0.3):
+        got = ocs_lib.activate(x, exp, ov, opts + " --precision=" + prec)
+        ref = orc.fp64_stft(x, exp, ov, opts)
+        err = orc.rel_l2(got, ref)
+        assert err <= bar, (prec, exp, ov, opts, err)
+
+
+def test_tc_bf16_needs_short_advance(ocs_lib):
+    with pytest.raises(ocs_lib.OcsError, match="frame advance"):
+        ocs_lib.activate(signal(1, 50000), 10, -0.5, "--precision=tc-bf16x3")
 
 
 def test_tc_rejects_unsupported_window(ocs_lib):
