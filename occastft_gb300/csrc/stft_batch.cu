@@ -18,15 +18,31 @@ __host__ __device__ constexpr size_t batch_group_smem(int exp)
 {
     return (size_t)fused_fpc(exp) * fused_buf_stride(exp) * 8 + (size_t)(256 / 32) * 4 + 16;
 }
-__host__ __device__ constexpr size_t batch_smem_ct()
+__host__ __device__ constexpr size_t batch_frames_smem()
 {
     size_t m = 0;
     for (int e = kBatchMinExp; e <= kBatchMaxExp; ++e) m = batch_group_smem(e) > m ? batch_group_smem(e) : m;
+    return (m + 15) / 16 * 16;
+}
+// Twiddle and window tables of windows up to 2^11 are copied into shared
+// memory behind the frame buffers (and re-copied only when a tile's plan or
+// window table differs from the previous tile's); larger windows read theirs
+// through L1.
+constexpr int kBatchSmemTabMaxExp = 11;
+__host__ __device__ constexpr size_t batch_tab_smem()
+{
+    size_t m = 0;
+    for (int e = kBatchMinExp; e <= kBatchSmemTabMaxExp; ++e) {
+        const size_t b = (size_t)fused_tw_size(e) * 8 + ((size_t)1 << e) * 4;
+        m = b > m ? b : m;
+    }
     return m;
 }
+__host__ __device__ constexpr size_t batch_smem_ct() { return batch_frames_smem() + batch_tab_smem(); }
 
 template <int EXP>
-__device__ __forceinline__ void batch_tile(const FusedArgs& a, uint64_t f0, uint32_t nf, float2* smem)
+__device__ __forceinline__ void batch_tile(const FusedArgs& a, uint64_t f0, uint32_t nf, float2* smem,
+                                           const float2** s_tw, const float** s_win)
 {
     static_assert(fused_cta_threads(EXP) == 256, "batch CTAs have 256 threads");
     using K = Core<EXP>;
@@ -38,11 +54,30 @@ __device__ __forceinline__ void batch_tile(const FusedArgs& a, uint64_t f0, uint
     const int t = tid - lf * T;
     float2* buf = smem + lf * BS;
     float* red = reinterpret_cast<float*>(smem + FPC * BS);
+    const float2* tw = a.tw;
+    const float2* win2 = reinterpret_cast<const float2*>(a.win);
+    if constexpr (EXP <= kBatchSmemTabMaxExp) {
+        constexpr int TWN = fused_tw_size(EXP);
+        float2* st = reinterpret_cast<float2*>(reinterpret_cast<char*>(smem) + batch_frames_smem());
+        float2* sw = st + TWN;
+        // every thread sees the same pointers: a uniform branch
+        if (*s_tw != a.tw || *s_win != a.win) {
+            __syncthreads();  // the previous tile's table reads are over
+            for (int i = tid; i < TWN; i += 256) st[i] = a.tw[i];
+            for (int i = tid; i < (1 << EXP) / 2; i += 256) sw[i] = win2[i];
+            __syncthreads();
+            if (tid == 0) {
+                *s_tw = a.tw;
+                *s_win = a.win;
+            }
+        }
+        tw = st;
+        win2 = sw;
+    }
     FusedArgs b = a;
     b.frames = f0 + nf;  // frames past the tile belong to the next tile
     for (uint64_t fb = f0; fb < f0 + nf; fb += FPC)
-        fused_group_frames<EXP, OUT_RUNTIME>(b, fb, buf, red, a.tw, reinterpret_cast<const float2*>(a.win), tid, lf,
-                                             t);
+        fused_group_frames<EXP, OUT_RUNTIME>(b, fb, buf, red, tw, win2, tid, lf, t);
 }
 
 __global__ void __launch_bounds__(256, 2)
@@ -51,6 +86,12 @@ stft_batch_kernel(const FusedArgs* __restrict__ reqs, const BatchTile* __restric
 {
     extern __shared__ float2 smem[];
     __shared__ uint32_t s_tile;
+    __shared__ const float2* s_tw;  // tables now in shared memory (see batch_tile)
+    __shared__ const float* s_win;
+    if (threadIdx.x == 0) {
+        s_tw = nullptr;
+        s_win = nullptr;
+    }
     const uint32_t nt = *ntiles;
     for (;;) {
         if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1u);
@@ -61,14 +102,14 @@ stft_batch_kernel(const FusedArgs* __restrict__ reqs, const BatchTile* __restric
         const BatchTile tl = tiles[ti];
         const FusedArgs a = reqs[tl.req];
         switch (a.exp) {
-        case 6: batch_tile<6>(a, tl.f0, tl.nframes, smem); break;
-        case 7: batch_tile<7>(a, tl.f0, tl.nframes, smem); break;
-        case 8: batch_tile<8>(a, tl.f0, tl.nframes, smem); break;
-        case 9: batch_tile<9>(a, tl.f0, tl.nframes, smem); break;
-        case 10: batch_tile<10>(a, tl.f0, tl.nframes, smem); break;
-        case 11: batch_tile<11>(a, tl.f0, tl.nframes, smem); break;
-        case 12: batch_tile<12>(a, tl.f0, tl.nframes, smem); break;
-        case 13: batch_tile<13>(a, tl.f0, tl.nframes, smem); break;
+        case 6: batch_tile<6>(a, tl.f0, tl.nframes, smem, &s_tw, &s_win); break;
+        case 7: batch_tile<7>(a, tl.f0, tl.nframes, smem, &s_tw, &s_win); break;
+        case 8: batch_tile<8>(a, tl.f0, tl.nframes, smem, &s_tw, &s_win); break;
+        case 9: batch_tile<9>(a, tl.f0, tl.nframes, smem, &s_tw, &s_win); break;
+        case 10: batch_tile<10>(a, tl.f0, tl.nframes, smem, &s_tw, &s_win); break;
+        case 11: batch_tile<11>(a, tl.f0, tl.nframes, smem, &s_tw, &s_win); break;
+        case 12: batch_tile<12>(a, tl.f0, tl.nframes, smem, &s_tw, &s_win); break;
+        case 13: batch_tile<13>(a, tl.f0, tl.nframes, smem, &s_tw, &s_win); break;
         default: break;
         }
     }
