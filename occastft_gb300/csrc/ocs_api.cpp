@@ -186,8 +186,9 @@ int get_window(int kind, int exp, float sigma, bool scaled, const float** out)
 
 // ---------------------------------------------------------------- kernel choice
 // Variants of the fused kernel: 0 one frame per FFT, direct I/O; 1 one frame
-// per FFT, shared-memory staged I/O (windows <= 2^9); 2 two frames per FFT.
-enum { VAR_DIRECT = 0, VAR_STAGED = 1, VAR_PAIR = 2 };
+// per FFT, shared-memory staged I/O (windows <= 2^9); 2 two frames per FFT;
+// 3 one lane per frame (window 2^6, power outputs).
+enum { VAR_DIRECT = 0, VAR_STAGED = 1, VAR_PAIR = 2, VAR_TPF = 3, VAR_COUNT = 4 };
 
 bool env_is(const char* name, const char* val)
 {
@@ -199,7 +200,7 @@ bool env_is(const char* name, const char* val)
 int default_variant(int exp, int outk)
 {
     const bool power = outk != ocs::OUT_HALF;
-    if (exp == 6) return VAR_STAGED;
+    if (exp == 6) return power ? VAR_TPF : VAR_STAGED;
     if (power && (exp == 9 || exp == 13 || exp == 14)) return VAR_PAIR;
     if (!power && (exp == 13 || exp == 14)) return VAR_PAIR;
     return VAR_DIRECT;
@@ -210,6 +211,8 @@ bool variant_ok(int v, int exp, int outk, bool out16)
     if (v == VAR_PAIR) return ocs::pair_has(exp) && outk != ocs::OUT_PLANES && !env_is("OCS_KERNEL", "single");
     if (v == VAR_STAGED)
         return ocs::fused_has_staged(exp) && outk != ocs::OUT_PLANES && out16 && !env_is("OCS_IO_SCHEME", "direct");
+    if (v == VAR_TPF)
+        return ocs::tpf_has(exp, outk) && out16 && !env_is("OCS_IO_SCHEME", "direct") && !env_is("OCS_KERNEL", "single");
     return true;
 }
 
@@ -259,14 +262,17 @@ int grid_size(int exp, int outk, int variant, uint64_t frames)
         auto key = std::make_pair(exp, outk * 4 + variant);
         auto it = c.occupancy.find(key);
         if (it == c.occupancy.end()) {
-            occ = std::max(1, variant == 2 ? ocs::pair_occupancy(exp, outk)
-                                           : ocs::fused_occupancy(exp, outk, variant == 1));
+            occ = std::max(1, variant == VAR_PAIR  ? ocs::pair_occupancy(exp, outk)
+                              : variant == VAR_TPF ? ocs::tpf_occupancy(exp, outk)
+                                                   : ocs::fused_occupancy(exp, outk, variant == VAR_STAGED));
             c.occupancy[key] = occ;
         } else {
             occ = it->second;
         }
     }
-    const uint64_t fpc = (uint64_t)(variant == VAR_PAIR ? 2 * ocs::pair_per_cta(exp) : ocs::fused_frames_per_cta(exp));
+    const uint64_t fpc = (uint64_t)(variant == VAR_PAIR  ? 2 * ocs::pair_per_cta(exp)
+                                    : variant == VAR_TPF ? ocs::tpf_frames_per_cta()
+                                                         : ocs::fused_frames_per_cta(exp));
     const uint64_t need = (frames + fpc - 1) / fpc;
     const uint64_t full = (uint64_t)c.sms * occ;
     return (int)std::max<uint64_t>(1, std::min(need, full));
@@ -299,6 +305,7 @@ cudaError_t launch_variant(int v, const Request& r, int outk, ocs::FusedArgs a, 
         a.tw = tw_pair;
         return ocs::launch_pair(r.exp, outk, a, grid_size(r.exp, outk, VAR_PAIR, a.frames), st);
     }
+    if (v == VAR_TPF) return ocs::launch_tpf(r.exp, outk, a, grid_size(r.exp, outk, VAR_TPF, a.frames), st);
     a.tw = tw_single;
     return ocs::launch_fused(r.exp, outk, v == VAR_STAGED, a, grid_size(r.exp, outk, v, a.frames), st);
 }
@@ -442,9 +449,13 @@ int launch_frames(const Request& r, const float* d_sig, uint64_t n, float* d_out
         return OCS_OK;
     }
 
-    int cand[3], nc = 0;
-    for (int v = 0; v < 3; ++v)
+    int cand[VAR_COUNT], nc = 0;
+    for (int v = 0; v < VAR_COUNT; ++v)
         if (variant_ok(v, r.exp, outk, out16)) cand[nc++] = v;
+    if (env_is("OCS_KERNEL", "tpf") && variant_ok(VAR_TPF, r.exp, outk, out16)) {
+        OCS_CUDA(launch_variant(VAR_TPF, r, outk, a, tw_single, tw_pair, st));
+        return OCS_OK;
+    }
     int choice = default_variant(r.exp, outk);
     bool have = false;
     for (int i = 0; i < nc; ++i) have |= cand[i] == choice;

@@ -63,6 +63,12 @@ size_t batch_smem_bytes();
 cudaError_t launch_batch(const FusedArgs* d_reqs, const BatchTile* d_tiles, const uint32_t* d_ntiles,
                          uint32_t* d_counter, int grid, cudaStream_t st);
 
+// thread-per-frame kernel (window 2^6, power outputs)
+bool tpf_has(int exp, int outk);
+int tpf_frames_per_cta();
+int tpf_occupancy(int exp, int outk);
+cudaError_t launch_tpf(int exp, int outk, const FusedArgs& a, int grid, cudaStream_t st);
+
 // windows 2^16 .. 2^22: four-step FFT in two launches (column pass, row pass)
 constexpr int kLargeMinExp = 16;
 constexpr int kLargeMaxExp = 22;

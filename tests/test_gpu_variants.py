@@ -34,6 +34,7 @@ print(json.dumps(res))
 
 
 @pytest.mark.parametrize("env", [
+    {"OCS_KERNEL": "tpf", "OCS_AUTOTUNE": "0"},
     {"OCS_KERNEL": "single", "OCS_IO_SCHEME": "direct", "OCS_AUTOTUNE": "0"},
     {"OCS_KERNEL": "single", "OCS_AUTOTUNE": "0"},
     {"OCS_AUTOTUNE": "0"},
