@@ -102,9 +102,43 @@ __host__ __device__ constexpr int staged_out_stride(int exp, int outk)
     return (outk == OUT_HALF ? 2 * (1 << exp) : (1 << exp)) + 4;
 }
 
+// Above that exponent the plan table (~8 x 2^exp bytes) does not fit next to
+// the exchange buffers; the kernels then rebuild every twiddle from a
+// two-level table in shared memory: W_N^e = lo[e % 128] * hi[e / 128].
+__host__ __device__ constexpr size_t fused_tw2_entries(int exp) { return 128 + ((size_t)1 << exp) / 128; }
 __host__ __device__ constexpr size_t fused_tab_bytes(int exp)
 {
-    return fused_tables_in_smem(exp) ? (size_t)fused_tw_size(exp) * 8 + (size_t)fused_M(exp) * 8 : 0;
+    return fused_tables_in_smem(exp) ? (size_t)fused_tw_size(exp) * 8 + (size_t)fused_M(exp) * 8
+                                     : fused_tw2_entries(exp) * 8;
+}
+
+struct TwTwoLevel {
+    const float2* lo;  // W_N^e, e < 128
+    const float2* hi;  // W_N^(128 h), h < N / 128
+};
+// twiddle W_N^e that the plan table holds at index idx
+__device__ __forceinline__ float2 tw_get(const float2* tw, int idx, int /*e*/) { return tw[idx]; }
+__device__ __forceinline__ float2 tw_get(const TwTwoLevel& tw, int /*idx*/, int e)
+{
+    return cmul(tw.lo[e & 127], tw.hi[e >> 7]);
+}
+// Fills the two-level table from the plan table, whose first M entries are
+// W_N^k (k < M); W_N^(k + M) = -W_N^k.
+template <int EXP>
+__device__ __forceinline__ TwTwoLevel build_tw2(const float2* plan, float2* s, int tid, int nthreads)
+{
+    constexpr int M = fused_M(EXP), NH = (1 << EXP) / 128;
+    for (int i = tid; i < 128 + NH; i += nthreads) {
+        float2 w;
+        if (i < 128) {
+            w = plan[i];
+        } else {
+            const int e = 128 * (i - 128);
+            w = e < M ? plan[e] : make_float2(-plan[e - M].x, -plan[e - M].y);
+        }
+        s[i] = w;
+    }
+    return TwTwoLevel{s, s + 128};
 }
 
 __host__ __device__ constexpr size_t fused_smem_bytes_ct(int exp)
@@ -168,8 +202,10 @@ struct Core {
         }
     }
 
-    // all Stockham stages; the last stage leaves Z[t + u*T] in slot u
-    static __device__ __forceinline__ void fft(float2 (&v)[R], float2* buf, const float2* tw, int t)
+    // all Stockham stages; the last stage leaves Z[t + u*T] in slot u.
+    // TW: the plan table (const float2*) or a TwTwoLevel
+    template <typename TW>
+    static __device__ __forceinline__ void fft(float2 (&v)[R], float2* buf, const TW& tw, int t)
     {
         {
             constexpr int r = C.radix[0];
@@ -185,6 +221,7 @@ struct Core {
             constexpr int r = C.radix[s];
             constexpr int ns = fused_Ns(EXP, s);
             constexpr int toff = fused_tw_offset(EXP, s);
+            constexpr int ef = N / (ns * r);  // W_{ns r}^{j m} = W_N^{j m ef}
             group_sync<T>();
             // write the previous stage's outputs at their Stockham positions
             static_for<0, R / rp>([&](auto qc) {
@@ -205,7 +242,7 @@ struct Core {
                 const int j = (t + q * T) % ns;
                 static_for<1, r>([&](auto mc) {
                     constexpr int m = decltype(mc)::value;
-                    v[q + m * (R / r)] = cmul(v[q + m * (R / r)], tw[toff + (m - 1) * ns + j]);
+                    v[q + m * (R / r)] = cmul(v[q + m * (R / r)], tw_get(tw, toff + (m - 1) * ns + j, j * m * ef));
                 });
                 dft_inreg<R, r, q, R / r>(v);
             });
@@ -275,9 +312,9 @@ __device__ __forceinline__ void load_tables(const FusedArgs& a, float2* s_tab, i
 // One CTA-iteration: frames [fbase + lf] for every frame group of the CTA.
 // OUTK may be OUT_RUNTIME, in which case a.outk selects the output kind
 // (the batch kernel mixes requests of different kinds).
-template <int EXP, int OUTK>
+template <int EXP, int OUTK, typename TW = const float2*>
 __device__ __forceinline__ void fused_group_frames(const FusedArgs& a, uint64_t fbase, float2* buf, float* red,
-                                                   const float2* tw, const float2* win2, int tid, int lf, int t)
+                                                   const TW& tw, const float2* win2, int tid, int lf, int t)
 {
     using K = Core<EXP>;
     constexpr int N = K::N, M = K::M, R = K::R, T = K::T;
@@ -332,7 +369,7 @@ __device__ __forceinline__ void fused_group_frames(const FusedArgs& a, uint64_t 
         if (!active) return;
         const int k = t + u * T;
         float2 e, wo;
-        K::untangle(v[u], pu, tw[k], e, wo);
+        K::untangle(v[u], pu, tw_get(tw, k, k), e, wo);
         const float2 xa = cadd(e, wo);  // X[k]
         if (outk == OUT_POWER || outk == OUT_POWER_SERIAL) {
             const bool ser = OUTK == OUT_POWER_SERIAL || (OUTK == OUT_RUNTIME && outk == OUT_POWER_SERIAL);
@@ -387,11 +424,19 @@ stft_fused_kernel(const FusedArgs a)
     float2* buf = smem + lf * BS;
     float2* s_tab = smem + FPC * BS;
     float* red = reinterpret_cast<float*>(reinterpret_cast<char*>(s_tab) + fused_tab_bytes(EXP));
-    const float2* tw;
-    const float2* win2;
-    load_tables<EXP>(a, s_tab, tid, tw, win2);
-    for (uint64_t fbase = (uint64_t)blockIdx.x * FPC; fbase < a.frames; fbase += (uint64_t)gridDim.x * FPC)
-        fused_group_frames<EXP, OUTK>(a, fbase, buf, red, tw, win2, tid, lf, t);
+    if constexpr (fused_tables_in_smem(EXP)) {
+        const float2* tw;
+        const float2* win2;
+        load_tables<EXP>(a, s_tab, tid, tw, win2);
+        for (uint64_t fbase = (uint64_t)blockIdx.x * FPC; fbase < a.frames; fbase += (uint64_t)gridDim.x * FPC)
+            fused_group_frames<EXP, OUTK>(a, fbase, buf, red, tw, win2, tid, lf, t);
+    } else {
+        const TwTwoLevel tw = build_tw2<EXP>(a.tw, s_tab, tid, blockDim.x);
+        __syncthreads();
+        const float2* win2 = reinterpret_cast<const float2*>(a.win);
+        for (uint64_t fbase = (uint64_t)blockIdx.x * FPC; fbase < a.frames; fbase += (uint64_t)gridDim.x * FPC)
+            fused_group_frames<EXP, OUTK>(a, fbase, buf, red, tw, win2, tid, lf, t);
+    }
 }
 
 // ============================================================ staged I/O kernel
@@ -492,7 +537,7 @@ stft_staged_kernel(const FusedArgs a)
             else pu = K::template partner_at<u>(v, buf, t, src);
             const int k = t + u * T;
             float2 e, wo;
-            K::untangle(v[u], pu, tw[k], e, wo);
+            K::untangle(v[u], pu, tw_get(tw, k, k), e, wo);
             const float2 xa = cadd(e, wo);
             if constexpr (OUTK == OUT_HALF) {
                 float2* o2 = reinterpret_cast<float2*>(orow);
