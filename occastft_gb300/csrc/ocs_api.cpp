@@ -196,16 +196,19 @@ bool env_is(const char* name, const char* val)
     return e && std::strcmp(e, val) == 0;
 }
 
-// defaults measured on GB300 (1e8 samples, overlap 0.5) for when tuning is off
+// defaults measured on GB300 (1e8 samples, overlap 0.5, the autotuner's own
+// picks) for when tuning is off or the stream is being captured
 int default_variant(int exp, int outk)
 {
     const bool power = outk != ocs::OUT_HALF;
-    if (exp == 6) return power ? VAR_TPF : VAR_STAGED;
-    if (power && (exp == 9 || exp == 13 || exp == 14)) return VAR_PAIR;
-    if (!power && (exp == 13 || exp == 14)) return VAR_PAIR;
+    if (power) {
+        if (exp == 6) return VAR_TPF;
+        if (exp == 9 || exp == 10 || exp == 12 || exp == 13 || exp == 14) return VAR_PAIR;
+        return VAR_DIRECT;
+    }
+    if (exp == 6 || exp == 13 || exp == 14) return VAR_PAIR;
     return VAR_DIRECT;
 }
-
 bool variant_ok(int v, int exp, int outk, bool out16)
 {
     if (v == VAR_PAIR) return ocs::pair_has(exp) && outk != ocs::OUT_PLANES && !env_is("OCS_KERNEL", "single");
