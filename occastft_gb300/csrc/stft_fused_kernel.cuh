@@ -476,6 +476,24 @@ stft_staged_kernel(const FusedArgs a)
 
     // issue the async copies of tile [f0, f0 + FPC)
     auto prefetch = [&](uint64_t f0) {
+        if (cs == 16) {
+            // N / 4 chunks per row, a compile-time count: no division per copy
+            constexpr int CPR = N / 4;
+            for (int q = tid; q < FPC * CPR; q += NT) {
+                const int jj = q / CPR;
+                const int col = q - jj * CPR;
+                const uint64_t f = f0 + jj;
+                const uint64_t pos = f * a.hop + (uint64_t)col * 4;
+                int bytes = 0;
+                if (f < a.frames && pos < a.n) {
+                    const uint64_t left = a.n - pos;
+                    bytes = left >= 4 ? 16 : (int)left * 4;
+                }
+                cp_async(s_in + jj * IS + col * 4, bytes ? a.x + pos : a.x, bytes, 16);
+            }
+            cp_async_commit();
+            return;
+        }
         const int chunks = N / per_chunk;
         for (int q = tid; q < FPC * chunks; q += NT) {
             const int jj = q / chunks;

@@ -54,16 +54,39 @@ __global__ void __launch_bounds__(kTpfThreads, 2) stft_tpf_kernel(const FusedArg
     for (uint64_t g = (uint64_t)blockIdx.x * (kTpfThreads / 32) + warp; g * 32 < a.frames; g += wstride) {
         const uint64_t f0 = g * 32;
         // ---------------- 32 frames -> 32 rows
-        for (int q = lane; q < 32 * chunks; q += 32) {
-            const int jj = q / chunks, col = q - jj * chunks;
-            const uint64_t f = f0 + jj;
-            const uint64_t pos = f * a.hop + (uint64_t)col * per_chunk;
-            int bytes = 0;
-            if (f < a.frames && pos < a.n) {
-                const uint64_t left = a.n - pos;
-                bytes = left >= (uint64_t)per_chunk ? cs : (int)left * 4;
+        if (cs == 16) {
+            // N / 4 chunks per row: a lane keeps its column, rows advance by
+            // 32 / (N / 4) per step, so the addresses are plain increments
+            constexpr int CPR = N / 4, RSTEP = 32 / CPR;
+            const int col = lane % CPR, j0 = lane / CPR;
+            uint64_t f = f0 + j0;
+            uint64_t pos = f * a.hop + (uint64_t)col * 4;
+            const uint64_t pstep = (uint64_t)RSTEP * a.hop;
+            float* dst = rows + j0 * RS + col * 4;
+#pragma unroll 4
+            for (int it = 0; it < 32 / RSTEP; ++it) {
+                int bytes = 0;
+                if (f < a.frames && pos < a.n) {
+                    const uint64_t left = a.n - pos;
+                    bytes = left >= 4 ? 16 : (int)left * 4;
+                }
+                cp_async(dst, bytes ? a.x + pos : a.x, bytes, 16);
+                f += RSTEP;
+                pos += pstep;
+                dst += RSTEP * RS;
             }
-            cp_async(rows + jj * RS + col * per_chunk, bytes ? a.x + pos : a.x, bytes, cs);
+        } else {
+            for (int q = lane; q < 32 * chunks; q += 32) {
+                const int jj = q / chunks, col = q - jj * chunks;
+                const uint64_t f = f0 + jj;
+                const uint64_t pos = f * a.hop + (uint64_t)col * per_chunk;
+                int bytes = 0;
+                if (f < a.frames && pos < a.n) {
+                    const uint64_t left = a.n - pos;
+                    bytes = left >= (uint64_t)per_chunk ? cs : (int)left * 4;
+                }
+                cp_async(rows + jj * RS + col * per_chunk, bytes ? a.x + pos : a.x, bytes, cs);
+            }
         }
         cp_async_commit();
         cp_async_wait_all();
