@@ -207,7 +207,7 @@ int default_variant(int exp, int outk)
         return VAR_DIRECT;
     }
     if (exp == 6) return VAR_STAGED;
-    if (exp == 13 || exp == 14) return VAR_PAIR;
+    if (exp == 14) return VAR_PAIR;
     return VAR_DIRECT;
 }
 bool variant_ok(int v, int exp, int outk, bool out16)
