@@ -105,6 +105,19 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
@@ -939,16 +952,6 @@ __global__ void __launch_bounds__(kTc2Threads, 1)
             }
             fence_after();
             const float scale = sB[s * FPT + lf];
-            float y[C::NO];
-#pragma unroll
-            for (int cb = 0; cb < C::NO / 32; ++cb) {
-                float t[32];
-                tmem_ld32(tmem + s * C::NO + lane_base + cb * 32, t);
-#pragma unroll
-                for (int q = 0; q < 32; ++q) y[cb * 32 + q] = t[q];
-            }
-            fence_before();
-            mbar_arrive(&bar[B_D1_EMPTY + s]);
             const int s2 = (int)(i % C::NA2);  // A2 slot
             const uint32_t use2 = (uint32_t)(i / C::NA2);
             const bool ok2 = i < (uint64_t)C::NA2 || mbar_wait_t(&bar[B_A2_EMPTY + s2], (use2 - 1) & 1, abort_flag);
@@ -958,14 +961,18 @@ __global__ void __launch_bounds__(kTc2Threads, 1)
             }
             if (g == 0) sC[s2 * FPT + lf] = scale;
             unsigned char* a2 = A2 + s2 * C::A2_BYTES;
-#pragma unroll
+            // eight k1 (sixteen accumulator columns) per step, the loop kept
+            // rolled: the four warp roles run different code at the same time
+            // and instruction fetch was what limited the kernel
+#pragma unroll 1
             for (int k1b = 0; k1b < R; k1b += 8) {
+                float t[16];
+                tmem_ld16(tmem + s * C::NO + lane_base + 2 * k1b, t);
                 float re[8], im[8];
 #pragma unroll
                 for (int q = 0; q < 8; ++q) {
-                    const int k1 = k1b + q;
-                    const float2 w = TW[k1 * R + g];  // W_N^{g k1} / R
-                    const float yr = y[2 * k1], yi = y[2 * k1 + 1];
+                    const float2 w = TW[(k1b + q) * R + g];  // W_N^{g k1} / R
+                    const float yr = t[2 * q], yi = t[2 * q + 1];
                     re[q] = yr * w.x - yi * w.y;
                     im[q] = yr * w.y + yi * w.x;
                 }
@@ -980,6 +987,8 @@ __global__ void __launch_bounds__(kTc2Threads, 1)
                     *reinterpret_cast<uint4*>(a2 + k * C::A2_PART + oi_) = pi[k];
                 }
             }
+            fence_before();
+            mbar_arrive(&bar[B_D1_EMPTY + s]);
             fence_async_smem();
             mbar_arrive(&bar[B_A2_FULL + s2]);
         }
@@ -997,37 +1006,33 @@ __global__ void __launch_bounds__(kTc2Threads, 1)
             }
             fence_after();
             const float back = sD[s * FPT + lf] * (float)R;  // undo both scalings (powers of two)
-            float xs[C::NO];
-#pragma unroll
-            for (int cb = 0; cb < C::NO / 32; ++cb) {
-                float t[32];
-                tmem_ld32(tmem + 2 * C::NO + s * C::NO + lane_base + cb * 32, t);
-#pragma unroll
-                for (int q = 0; q < 32; ++q) xs[cb * 32 + q] = t[q];
-            }
-            fence_before();
-            mbar_arrive(&bar[B_D2_EMPTY + s]);
             const uint64_t f = tile_of(j) * FPT + lf;
-            if (f < a.frames) {
-                if constexpr (OUTK == OUT_HALF) {
-                    float2* o2 = reinterpret_cast<float2*>(a.out);
+            const bool act = f < a.frames;
+            // eight k2 per step, rolled (see epilogue 1); the accumulator loads
+            // run on every lane (they are warp-collective), the stores only
+            // for rows of real frames
+            constexpr int K2END = OUTK == OUT_HALF ? R : R / 2 + 1;
+#pragma unroll 1
+            for (int k2b = 0; k2b < K2END; k2b += 8) {
+                float t[16];
+                tmem_ld16(tmem + 2 * C::NO + s * C::NO + lane_base + 2 * k2b, t);
 #pragma unroll
-                    for (int k2 = 0; k2 < R; ++k2) {
-                        const int k = k1 + R * k2;
-                        const float2 X = make_float2(xs[2 * k2] * back, xs[2 * k2 + 1] * back);
+                for (int q = 0; q < 8; ++q) {
+                    const int k2 = k2b + q;
+                    if (!act || k2 >= K2END) break;
+                    const int k = k1 + R * k2;
+                    const float xr = t[2 * q] * back, xi = t[2 * q + 1] * back;
+                    if constexpr (OUTK == OUT_HALF) {
+                        float2* o2 = reinterpret_cast<float2*>(a.out);
+                        const float2 X = make_float2(xr, xi);
                         if (!a.dense) {
                             const uint64_t flat = f * (uint64_t)N + k;
                             if (flat < a.ohalf) __stcs(o2 + flat, X);
                         } else if (k <= N / 2) {
                             __stcs(o2 + f * (uint64_t)(N / 2 + 1) + k, X);
                         }
-                    }
-                } else {
-#pragma unroll
-                    for (int k2 = 0; k2 <= R / 2; ++k2) {
-                        const int k = k1 + R * k2;
+                    } else {
                         if (k > N / 2) continue;
-                        const float xr = xs[2 * k2] * back, xi = xs[2 * k2 + 1] * back;
                         const float p = (OUTK == OUT_POWER_SERIAL) ? fabsf(xr) * 1.41421356237309505f
                                                                    : sqrtf(xr * xr + xi * xi);
                         if (!a.dense) {
@@ -1040,6 +1045,8 @@ __global__ void __launch_bounds__(kTc2Threads, 1)
                     }
                 }
             }
+            fence_before();
+            mbar_arrive(&bar[B_D2_EMPTY + s]);
         }
     }
     __syncwarp();
