@@ -1061,30 +1061,40 @@ __global__ void __launch_bounds__(kTc2Threads, 1)
 template <int R, int PM>
 const unsigned char* tc_tables(cudaError_t* e)
 {
-    // built once per process (one device per runner context)
-    static std::once_flag once;
-    static cudaError_t built = cudaSuccess;
+    // built once per process (one device per runner context); a failed build
+    // (say, attempted while another stream was capturing a graph) is retried
+    // by the next call instead of being remembered
+    static std::mutex mu;
+    static bool built = false;
     static unsigned char* img = nullptr;
-    std::call_once(once, [&] {
-        void* p = nullptr;
-        if constexpr (R == 16 && PM == 1) built = cudaGetSymbolAddress(&p, g_tc_tab16_1);
-        else if constexpr (R == 16 && PM == 2) built = cudaGetSymbolAddress(&p, g_tc_tab16_2);
-        else if constexpr (R == 16) built = cudaGetSymbolAddress(&p, g_tc_tab16_3);
-        else if constexpr (PM == 1) built = cudaGetSymbolAddress(&p, g_tc_tab32_1);
-        else if constexpr (PM == 2) built = cudaGetSymbolAddress(&p, g_tc_tab32_2);
-        else built = cudaGetSymbolAddress(&p, g_tc_tab32_3);
-        if (built != cudaSuccess) return;
-        img = static_cast<unsigned char*>(p);
+    std::lock_guard<std::mutex> lk(mu);
+    if (built) {
+        *e = cudaSuccess;
+        return img;
+    }
+    void* p = nullptr;
+    cudaError_t r;
+    if constexpr (R == 16 && PM == 1) r = cudaGetSymbolAddress(&p, g_tc_tab16_1);
+    else if constexpr (R == 16 && PM == 2) r = cudaGetSymbolAddress(&p, g_tc_tab16_2);
+    else if constexpr (R == 16) r = cudaGetSymbolAddress(&p, g_tc_tab16_3);
+    else if constexpr (PM == 1) r = cudaGetSymbolAddress(&p, g_tc_tab32_1);
+    else if constexpr (PM == 2) r = cudaGetSymbolAddress(&p, g_tc_tab32_2);
+    else r = cudaGetSymbolAddress(&p, g_tc_tab32_3);
+    if (r == cudaSuccess) {
         // a private stream: the caller's may be capturing a graph
         cudaStream_t s2 = nullptr;
-        built = cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking);
-        if (built != cudaSuccess) return;
-        build_tc_tables_kernel<R, PM><<<8, 256, 0, s2>>>(img);
-        built = cudaGetLastError();
-        if (built == cudaSuccess) built = cudaStreamSynchronize(s2);
-        cudaStreamDestroy(s2);
-    });
-    *e = built;
+        r = cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking);
+        if (r == cudaSuccess) {
+            build_tc_tables_kernel<R, PM><<<8, 256, 0, s2>>>(static_cast<unsigned char*>(p));
+            r = cudaGetLastError();
+            if (r == cudaSuccess) r = cudaStreamSynchronize(s2);
+            cudaStreamDestroy(s2);
+        }
+    }
+    *e = r;
+    if (r != cudaSuccess) return nullptr;
+    img = static_cast<unsigned char*>(p);
+    built = true;
     return img;
 }
 
