@@ -187,7 +187,7 @@ int get_window(int kind, int exp, float sigma, bool scaled, const float** out)
 // ---------------------------------------------------------------- kernel choice
 // Variants of the fused kernel: 0 one frame per FFT, direct I/O; 1 one frame
 // per FFT, shared-memory staged I/O (windows <= 2^9); 2 two frames per FFT;
-// 3 one lane per frame (window 2^6, power outputs).
+// 3 N/64 lanes per frame, the FFT in registers (windows 2^6 .. 2^8, power outputs).
 enum { VAR_DIRECT = 0, VAR_STAGED = 1, VAR_PAIR = 2, VAR_TPF = 3, VAR_COUNT = 4 };
 
 bool env_is(const char* name, const char* val)
@@ -202,7 +202,7 @@ int default_variant(int exp, int outk)
 {
     const bool power = outk != ocs::OUT_HALF;
     if (power) {
-        if (exp == 6) return VAR_TPF;
+        if (exp <= 8) return VAR_TPF;
         if (exp == 9 || exp == 10 || exp == 12 || exp == 13 || exp == 14) return VAR_PAIR;
         return VAR_DIRECT;
     }
@@ -275,7 +275,7 @@ int grid_size(int exp, int outk, int variant, uint64_t frames)
         }
     }
     const uint64_t fpc = (uint64_t)(variant == VAR_PAIR  ? 2 * ocs::pair_per_cta(exp)
-                                    : variant == VAR_TPF ? ocs::tpf_frames_per_cta()
+                                    : variant == VAR_TPF ? ocs::tpf_frames_per_cta(exp)
                                                          : ocs::fused_frames_per_cta(exp));
     const uint64_t need = (frames + fpc - 1) / fpc;
     const uint64_t full = (uint64_t)c.sms * occ;

@@ -65,7 +65,7 @@ cudaError_t launch_batch(const FusedArgs* d_reqs, const BatchTile* d_tiles, cons
 
 // thread-per-frame kernel (window 2^6, power outputs)
 bool tpf_has(int exp, int outk);
-int tpf_frames_per_cta();
+int tpf_frames_per_cta(int exp);
 int tpf_occupancy(int exp, int outk);
 cudaError_t launch_tpf(int exp, int outk, const FusedArgs& a, int grid, cudaStream_t st);
 

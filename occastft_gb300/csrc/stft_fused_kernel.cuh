@@ -87,6 +87,12 @@ __device__ __forceinline__ void cp_async(void* sdst, const void* gsrc, int bytes
         asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gsrc), "r"(bytes) : "memory");
     }
 }
+// a whole 16-byte chunk, no bounds (the caller checked the span)
+__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(sdst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 

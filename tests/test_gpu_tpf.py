@@ -1,7 +1,8 @@
-"""The thread-per-frame kernel (window 2^6, power outputs), forced with
-OCS_KERNEL=tpf, against the FP64 oracle: frame advances that are multiples
-of 4, 2 and 1 samples (16-, 8- and 4-byte copies), ragged signal ends, one
-frame, DC removal, the dense layout and the Serial runner's power."""
+"""The thread-per-frame kernels (power outputs; one lane per frame at window
+2^6, two and four lanes per frame at 2^7 and 2^8), forced with OCS_KERNEL=tpf,
+against the FP64 oracle: frame advances that are multiples of 4, 2 and 1
+samples (16-, 8- and 4-byte copies), ragged signal ends, one frame, DC
+removal, the dense layout and the Serial runner's power."""
 import numpy as np
 import pytest
 
@@ -16,23 +17,35 @@ def tpf(monkeypatch):
     monkeypatch.setenv("OCS_KERNEL", "tpf")
 
 
+@pytest.mark.parametrize("exp", [6, 7, 8])
 @pytest.mark.parametrize("n", [1, 63, 64, 1000, 4097, 1_000_003])
 @pytest.mark.parametrize("ov", [0.5, 0.75, 0.3, 0.33, 0.1])
-def test_tpf_sizes_and_advances(tpf, ocs_lib, orc, n, ov):
+def test_tpf_sizes_and_advances(tpf, ocs_lib, orc, exp, n, ov):
     x = signal(n % 1000 + 17, n)
     for opts in ("--hamming_window", "--hanning_window --remove_dc", "--blackman_window --layout=dense",
                  "--flattop_window --serial_power", "--nuttall_window --remove_dc --layout=dense"):
-        got = ocs_lib.activate(x, 6, ov, opts)
-        ref = orc.fp64_stft(x, 6, ov, opts)
+        got = ocs_lib.activate(x, exp, ov, opts)
+        ref = orc.fp64_stft(x, exp, ov, opts)
         assert got.size == ref.size
-        assert orc.rel_l2(got, ref) <= REL_L2, (n, ov, opts)
+        assert orc.rel_l2(got, ref) <= REL_L2, (exp, n, ov, opts)
 
 
-def test_tpf_matches_other_kernels(tpf, ocs_lib, monkeypatch):
+@pytest.mark.parametrize("exp", [7, 8])
+def test_tpf_large_dc_offset(tpf, ocs_lib, orc, exp):
+    """A signal sitting on a DC offset 1000 times its swing: only the frame's
+    first lane carries the mean, the others cancel it exactly."""
+    x = (signal(21, 200_003) * 1e-3 + 1.0).astype(np.float32)
+    got = ocs_lib.activate(x, exp, 0.5, "--hanning_window --remove_dc")
+    ref = orc.fp64_stft(x, exp, 0.5, "--hanning_window --remove_dc")
+    assert orc.rel_l2(got, ref) <= 1e-4
+
+
+@pytest.mark.parametrize("exp", [6, 7, 8])
+def test_tpf_matches_other_kernels(tpf, ocs_lib, monkeypatch, exp):
     """Same result as the cooperative kernels within the suite's cross-kernel
     tolerance."""
     x = signal(5, 3_000_017)
-    got = ocs_lib.activate(x, 6, 0.5, "--hanning_window --remove_dc")
+    got = ocs_lib.activate(x, exp, 0.5, "--hanning_window --remove_dc")
     monkeypatch.setenv("OCS_KERNEL", "single")
-    ref = ocs_lib.activate(x, 6, 0.5, "--hanning_window --remove_dc")
+    ref = ocs_lib.activate(x, exp, 0.5, "--hanning_window --remove_dc")
     np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-6 * float(np.abs(ref).max()))
