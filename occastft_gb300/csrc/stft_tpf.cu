@@ -273,9 +273,9 @@ struct TplCfg {
     static constexpr int M = N / 2;
     static constexpr int L = N / 64;      // lanes per frame
     static constexpr int F = 32 / L;      // frames per warp
-    static constexpr int RS = N + 4 * L;  // input row stride: 16-byte rows, the windowing pass
-                                          // (lane q of frame j at chunk L i + q) hits 8 distinct
-                                          // 16-byte bank groups per quarter-warp
+    // input row stride: an odd number of 16-byte units, so the rows that a
+    // warp's lanes read at the same column fall into distinct bank groups
+    static constexpr int RS = N + 4;
     static constexpr int ORS = N + L;     // output row stride (L j + q distinct banks)
     static constexpr int THREADS = 256;   // 8 warps; two CTAs per SM (128 registers)
     static constexpr size_t SMEM = (size_t)N * 4 + (size_t)(32 + 17) * L * 8 + (size_t)(THREADS / 32) * F * RS * 4;
@@ -372,23 +372,6 @@ __global__ void __launch_bounds__(TplCfg<EXP>::THREADS, 2) stft_tpfl_kernel(cons
         cp_async_wait_all();
         __syncwarp();
 
-        // ---------------- window in place: lane q takes the row's 16-byte chunks L i + q
-        {
-            float* wrow = rows + jf * RS + 4 * q;
-            const float* wwin = s_win + 4 * q;
-#pragma unroll
-            for (int i = 0; i < N / (4 * L); ++i) {
-                float4 d = *reinterpret_cast<const float4*>(wrow + 4 * L * i);
-                const float4 w = *reinterpret_cast<const float4*>(wwin + 4 * L * i);
-                d.x *= w.x;
-                d.y *= w.y;
-                d.z *= w.z;
-                d.w *= w.w;
-                *reinterpret_cast<float4*>(wrow + 4 * L * i) = d;
-            }
-        }
-        __syncwarp();
-
         // ---------------- radix-L split of the lane's frame (the whole row)
         float2 v[32];
         const float* row = rows + jf * RS;
@@ -398,8 +381,9 @@ __global__ void __launch_bounds__(TplCfg<EXP>::THREADS, 2) stft_tpfl_kernel(cons
 #pragma unroll
             for (int p = 0; p < L; ++p) {
                 const float4 d = *reinterpret_cast<const float4*>(row + 64 * p + 4 * c);
-                y0[p] = make_float2(d.x, d.y);
-                y1[p] = make_float2(d.z, d.w);
+                const float4 w = *reinterpret_cast<const float4*>(s_win + 64 * p + 4 * c);
+                y0[p] = make_float2(d.x * w.x, d.y * w.y);
+                y1[p] = make_float2(d.z * w.z, d.w * w.w);
             }
             if constexpr (L == 2) {
                 // z0 + (-1)^q z1
