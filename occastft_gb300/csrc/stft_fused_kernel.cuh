@@ -246,10 +246,29 @@ struct Core {
             static_for<0, R / r>([&](auto qc) {
                 constexpr int q = decltype(qc)::value;
                 const int j = (t + q * T) % ns;
-                static_for<1, r>([&](auto mc) {
-                    constexpr int m = decltype(mc)::value;
-                    v[q + m * (R / r)] = cmul(v[q + m * (R / r)], tw_get(tw, toff + (m - 1) * ns + j, j * m * ef));
-                });
+                if constexpr (std::is_same<TW, TwTwoLevel>::value) {
+                    // W^{j m ef} for m = 1, 2, ...: a two-level lookup every
+                    // 8th m and products with W^{j ef} in between (at most 7
+                    // rounding steps).  The lanes' lookups stride the lo table
+                    // by multiples of m ef, so each one costs several bank
+                    // wavefronts; this keeps one in eight.
+                    float2 b = make_float2(1.0f, 0.0f), w = b;
+                    static_for<1, r>([&](auto mc) {
+                        constexpr int m = decltype(mc)::value;
+                        if constexpr ((m - 1) % 8 == 0) {
+                            w = tw_get(tw, 0, j * m * ef);
+                            if constexpr (m == 1) b = w;
+                        } else {
+                            w = cmul(w, b);
+                        }
+                        v[q + m * (R / r)] = cmul(v[q + m * (R / r)], w);
+                    });
+                } else {
+                    static_for<1, r>([&](auto mc) {
+                        constexpr int m = decltype(mc)::value;
+                        v[q + m * (R / r)] = cmul(v[q + m * (R / r)], tw_get(tw, toff + (m - 1) * ns + j, j * m * ef));
+                    });
+                }
                 dft_inreg<R, r, q, R / r>(v);
             });
         });

@@ -54,9 +54,22 @@ __host__ __device__ constexpr int pair_ppc(int exp) { return pair_cta_threads(ex
 __host__ __device__ constexpr int pair_buf_stride(int exp) { return (1 << exp) + (1 << exp) / pair_R(exp) + 1; }
 __host__ __device__ constexpr bool pair_tables_in_smem(int exp) { return exp <= 11; }
 __host__ __device__ constexpr bool pair_supported(int exp) { return exp >= 6 && exp <= 14; }
+// Twiddle entries copied to shared memory: the whole table up to 2^11; above,
+// the first exchange stage's (31 x 32 entries, 7.9 KB), which next to the
+// window still fits beside the exchange buffers at the same occupancy; the
+// later stages' twiddles are read through L1.
+__host__ __device__ constexpr int pair_smem_tw_entries(int exp)
+{
+    return pair_tables_in_smem(exp) ? pair_tw_size(exp)
+                                    : (pair_cfg(exp).nstages > 2 ? pair_tw_offset(exp, 2) : pair_tw_size(exp));
+}
+// The window joins them except at 2^13: there its 32 KB would leave L1 too
+// small for the second stage's 57 KB of twiddles (measured 258 -> 240
+// Gsamples/s with it, and no better with the largest shared carveout).
+__host__ __device__ constexpr bool pair_smem_window(int exp) { return exp != 13; }
 __host__ __device__ constexpr size_t pair_tab_bytes(int exp)
 {
-    return pair_tables_in_smem(exp) ? (size_t)pair_tw_size(exp) * 8 + (size_t)(1 << exp) * 4 : 0;
+    return (size_t)pair_smem_tw_entries(exp) * 8 + (pair_smem_window(exp) ? (size_t)(1 << exp) * 4 : 0);
 }
 __host__ __device__ constexpr size_t pair_smem_bytes_ct(int exp)
 {
@@ -117,7 +130,10 @@ struct PairCore {
         }
     }
 
-    static __device__ __forceinline__ void fft(float2 (&v)[R], float2* buf, const float2* tw, int t)
+    // tws: shared-memory copy of the first pair_smem_tw_entries(EXP) twiddles;
+    // twg: the whole table in global memory (same indexing)
+    static __device__ __forceinline__ void fft(float2 (&v)[R], float2* buf, const float2* tws, const float2* twg,
+                                               int t)
     {
         {
             constexpr int r = C.radix[0];
@@ -133,6 +149,7 @@ struct PairCore {
             constexpr int r = C.radix[s];
             constexpr int ns = pair_Ns(EXP, s);
             constexpr int toff = pair_tw_offset(EXP, s);
+            const float2* const tw = pair_tw_offset(EXP, s + 1) <= pair_smem_tw_entries(EXP) ? tws : twg;
             group_sync<T>();
             static_for<0, R / rp>([&](auto qc) {
                 constexpr int q = decltype(qc)::value;
@@ -189,22 +206,19 @@ struct PairCore {
 };
 
 template <int EXP>
-__device__ __forceinline__ void pair_tables(const FusedArgs& a, float2* s_tab, int tid, const float2*& tw,
-                                            const float*& win)
+__device__ __forceinline__ void pair_tables(const FusedArgs& a, float2* s_tab, int tid, const float*& win)
 {
-    constexpr int TWN = pair_tw_size(EXP);
+    constexpr int TWN = pair_smem_tw_entries(EXP);
     constexpr int N = 1 << EXP;
-    if constexpr (pair_tables_in_smem(EXP)) {
-        for (int i = tid; i < TWN; i += blockDim.x) s_tab[i] = a.tw[i];
+    for (int i = tid; i < TWN; i += blockDim.x) s_tab[i] = a.tw[i];
+    if constexpr (pair_smem_window(EXP)) {
         float* sw = reinterpret_cast<float*>(s_tab + TWN);
         for (int i = tid; i < N; i += blockDim.x) sw[i] = a.win[i];
-        __syncthreads();
-        tw = s_tab;
         win = sw;
     } else {
-        tw = a.tw;
         win = a.win;
     }
+    __syncthreads();
 }
 
 template <int EXP, int OUTK>
@@ -224,9 +238,8 @@ stft_pair_kernel(const FusedArgs a)
     float2* buf = smem + lp * BS;
     float2* s_tab = smem + PPC * BS;
     float2* red = reinterpret_cast<float2*>(reinterpret_cast<char*>(s_tab) + pair_tab_bytes(EXP));
-    const float2* tw;
     const float* win;
-    pair_tables<EXP>(a, s_tab, tid, tw, win);
+    pair_tables<EXP>(a, s_tab, tid, win);
 
     const uint64_t pairs = (a.frames + 1) / 2;
     for (uint64_t pbase = (uint64_t)blockIdx.x * PPC; pbase < pairs; pbase += (uint64_t)gridDim.x * PPC) {
@@ -265,7 +278,7 @@ stft_pair_kernel(const FusedArgs a)
             }
         }
         if (a.remove_dc) K::remove_dc(v, red, tid, lp);
-        K::fft(v, buf, tw, t);
+        K::fft(v, buf, s_tab, a.tw, t);
         K::partners_prepare(v, buf, t);
         const int src = K::partner_lane(tid, t);
 
