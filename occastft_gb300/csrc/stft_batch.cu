@@ -26,8 +26,11 @@ __host__ __device__ constexpr size_t batch_frames_smem()
 }
 // Twiddle and window tables of windows up to 2^11 are copied into shared
 // memory behind the frame buffers (and re-copied only when a tile's plan or
-// window table differs from the previous tile's); larger windows read theirs
-// through L1.
+// window table differs from the previous tile's).  2^12 and 2^13 build the
+// two-level twiddle table there instead (128 + N/128 entries) and read their
+// window through L1: their full tables would take shared memory from L1,
+// which the frames' direct loads need (all windows measured slower with the
+// 2^12 tables resident).
 constexpr int kBatchSmemTabMaxExp = 11;
 __host__ __device__ constexpr size_t batch_tab_smem()
 {
@@ -76,8 +79,24 @@ __device__ __forceinline__ void batch_tile(const FusedArgs& a, uint64_t f0, uint
     }
     FusedArgs b = a;
     b.frames = f0 + nf;  // frames past the tile belong to the next tile
-    for (uint64_t fb = f0; fb < f0 + nf; fb += FPC)
-        fused_group_frames<EXP, OUT_RUNTIME>(b, fb, buf, red, tw, win2, tid, lf, t);
+    if constexpr (EXP > kBatchSmemTabMaxExp) {
+        float2* st = reinterpret_cast<float2*>(reinterpret_cast<char*>(smem) + batch_frames_smem());
+        if (*s_tw != a.tw || *s_win != nullptr) {
+            __syncthreads();  // the previous tile's table reads are over
+            build_tw2<EXP>(a.tw, st, tid, 256);
+            __syncthreads();
+            if (tid == 0) {
+                *s_tw = a.tw;
+                *s_win = nullptr;  // marks the region as holding a two-level table
+            }
+        }
+        const TwTwoLevel tw2{st, st + 128};
+        for (uint64_t fb = f0; fb < f0 + nf; fb += FPC)
+            fused_group_frames<EXP, OUT_RUNTIME>(b, fb, buf, red, tw2, win2, tid, lf, t);
+    } else {
+        for (uint64_t fb = f0; fb < f0 + nf; fb += FPC)
+            fused_group_frames<EXP, OUT_RUNTIME>(b, fb, buf, red, tw, win2, tid, lf, t);
+    }
 }
 
 __global__ void __launch_bounds__(256, 2)
