@@ -98,14 +98,18 @@ int large_m2_log2(int exp);
 cudaError_t build_two_level(float2* lo, float2* hi, uint64_t L, cudaStream_t st);
 cudaError_t launch_large(int exp, int outk, const LargeArgs& a, uint64_t frames, cudaStream_t st);
 
-// tensor-core split-precision form (tcgen05), windows 2^8 and 2^10
+// tensor-core split-precision form (tcgen05), windows 2^8 .. 2^12
 bool tc_supports(int exp);
+// whether split mode pm exists at window 2^exp (not the bf16 hi/mid/lo split
+// at 2^12, whose operands exceed shared memory)
+bool tc_mode_supported(int exp, int pm);
 // err: word the kernel sets to 1 when a pipeline wait gives up (after about a
 // second); test_stall: test hook, the first input phase of each CTA never
 // completes so that every wait runs out
-// pm: operand split, 1 fp16 hi/lo, 2 bf16 hi/lo, 3 bf16 hi/mid/lo.  The
-// pipelined kernel needs hop <= N (tc_piped); longer frame advances take the
-// first, fp16-only kernel.
+// pm: operand split, 1 fp16 hi/lo, 2 bf16 hi/lo, 3 bf16 hi/mid/lo.  At 2^8
+// and 2^10 the pipelined kernel needs hop <= N (tc_piped); longer frame
+// advances take the first, fp16-only kernel.  2^9, 2^11 and 2^12 run the
+// generic kernel, any advance.
 bool tc_piped(int exp, uint64_t hop);
 cudaError_t launch_tc(int exp, int outk, int pm, const FusedArgs& a, int* err, int test_stall, int sms,
                       cudaStream_t st);

@@ -118,6 +118,11 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ float2 cmul2(float2 a, float2 b)
+{
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
@@ -1058,6 +1063,373 @@ __global__ void __launch_bounds__(kTc2Threads, 1)
     }
 }
 
+// ============================================================ generic form
+// Windows N = P * Q with P >= Q: 512 = 32 x 16, 2048 = 64 x 32, 4096 = 64 x 64.
+// The same four-step DFT as above with n = g + Q m and k = k1 + P k2:
+//   pass 1  Y[g][k1] = sum_m y[g + Q m] W_P^{m k1}   GEMM rows (frame, g), K = m
+//   twiddle Y[g][k1] *= W_N^{g k1} / P
+//   pass 2  X[k1 + P k2] = sum_g Y[g][k1] W_Q^{g k2} GEMM rows (frame, k1), K = re/im of g
+// A tile is 128 / Q frames: 128 pass-1 rows and P / Q blocks of 128 pass-2
+// rows.  One CTA of 128 threads works one tile at a time (thread i owns TMEM
+// lane i): load + split, pass 1, epilogue 1, pass 2, epilogue 2.  A1 and A2
+// share one region (pass 1 has completed before A2 is written); B2 is stored
+// as 64-wide K panels; the twiddles come from a two-level table
+// W_N^e = lo[e & 63] * hi[e >> 6].  Every operand split of the pipelined form
+// is available where its operands fit in shared memory (the bf16 hi/mid/lo
+// split at 4096 does not: about 240 KB).
+template <int P, int Q, int PM>
+struct TcgCfg {
+    static constexpr int N = P * Q;
+    static constexpr int PARTS = Split<PM>::PARTS;
+    static constexpr int FPT = 128 / Q;         // frames per tile
+    static constexpr int MB = P / Q;            // pass-2 blocks of 128 rows
+    static constexpr int K1 = P, NO1 = 2 * P;   // pass 1
+    static constexpr int K2 = 2 * Q, NO2 = 2 * Q;  // pass 2
+    static constexpr int KP2 = (K2 + 63) / 64;  // B2 panels of 64 K
+    static constexpr uint32_t A1_PART = (K1 / 8) * 2048;  // 128 rows, MN-major
+    static constexpr uint32_t A2_PART = (K2 / 8) * 2048;
+    static constexpr uint32_t A1_BYTES = PARTS * A1_PART;
+    static constexpr uint32_t A2_BLOCK = PARTS * A2_PART;
+    static constexpr uint32_t A2_BYTES = MB * A2_BLOCK;
+    static constexpr uint32_t A_BYTES = A1_BYTES > A2_BYTES ? A1_BYTES : A2_BYTES;
+    static constexpr uint32_t B1_PART = NO1 * 128;  // K1 <= 64: one 128-byte row per output column
+    static constexpr uint32_t B2_PANEL = NO2 * 128;
+    static constexpr uint32_t B2_PART = KP2 * B2_PANEL;
+    static constexpr uint32_t B1_BYTES = PARTS * B1_PART;
+    static constexpr uint32_t B2_BYTES = PARTS * B2_PART;
+    static constexpr uint32_t OFF_A = 0;
+    static constexpr uint32_t OFF_B1 = OFF_A + A_BYTES;
+    static constexpr uint32_t OFF_B2 = OFF_B1 + B1_BYTES;
+    static constexpr uint32_t OFF_TW = OFF_B2 + B2_BYTES;  // 128 float2: lo[64], hi[64]
+    static constexpr uint32_t OFF_MISC = OFF_TW + 128 * 8;
+    static constexpr uint32_t SMEM = OFF_MISC + 256 + 1024;  // + slack to 1024-align the base
+    static constexpr uint32_t TMEM_USED = NO1 + MB * NO2;  // D1, then the D2 blocks
+    static constexpr uint32_t TMEM_COLS = TMEM_USED <= 128 ? 128 : 256;
+    static constexpr bool FITS = SMEM <= 227 * 1024;
+    static_assert(K1 <= 64 && P >= Q && P % Q == 0 && 128 % Q == 0 && N <= 4096, "shapes");
+    static_assert(TMEM_USED <= 256, "tensor memory");
+};
+
+template <int P, int Q, int OUTK, int PM>
+__global__ void __launch_bounds__(128, 1) stft_tcg_kernel(const FusedArgs a, int* err)
+{
+    using C = TcgCfg<P, Q, PM>;
+    using S = Split<PM>;
+    static_assert(C::FITS, "shared memory");
+    constexpr int N = C::N, FPT = C::FPT, PARTS = C::PARTS, MB = C::MB;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* sm = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    unsigned char* A = sm + C::OFF_A;
+    unsigned char* B1 = sm + C::OFF_B1;
+    unsigned char* B2 = sm + C::OFF_B2;
+    float2* TWL = reinterpret_cast<float2*>(sm + C::OFF_TW);
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + C::OFF_MISC);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + C::OFF_MISC + 16);
+    int* abort_flag = reinterpret_cast<int*>(sm + C::OFF_MISC + 24);
+    float* fscale = reinterpret_cast<float*>(sm + C::OFF_MISC + 32);  // FPT (<= 8) entries
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    // ---------------- set-up: barriers, tensor memory, DFT matrices, twiddles
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[0])));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[1])));
+        *abort_flag = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                     "r"(C::TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    // B1: rows 2k1 (re), 2k1+1 (im) of the real-input P-point DFT, K = m
+    for (int e = tid; e < C::NO1 * C::K1; e += 128) {
+        const int row = e / C::K1, m = e % C::K1, k1 = row >> 1;
+        double sn, cs;
+        sincospi(2.0 * (double)((m * k1) % P) / (double)P, &sn, &cs);
+        uint16_t pt[PARTS];
+        S::part1((row & 1) ? (float)(-sn) : (float)cs, pt);
+#pragma unroll
+        for (int k = 0; k < PARTS; ++k) *reinterpret_cast<uint16_t*>(B1 + k * C::B1_PART + k_off(row, m)) = pt[k];
+    }
+    // B2: the complex Q-point DFT as a real matrix, K = g (re part, k < Q) and g (im part, k >= Q)
+    for (int e = tid; e < C::NO2 * C::K2; e += 128) {
+        const int row = e / C::K2, k = e % C::K2, k2 = row >> 1, g = k % Q;
+        double sn, cs;
+        sincospi(2.0 * (double)((g * k2) % Q) / (double)Q, &sn, &cs);
+        // (yr + i yi)(c - i s): re = yr c + yi s, im = yi c - yr s
+        float w;
+        if ((row & 1) == 0) w = (k < Q) ? (float)cs : (float)sn;
+        else w = (k < Q) ? (float)(-sn) : (float)cs;
+        uint16_t pt[PARTS];
+        S::part1(w, pt);
+        const uint32_t off = (k >> 6) * C::B2_PANEL + k_off(row, k & 63);
+#pragma unroll
+        for (int q = 0; q < PARTS; ++q) *reinterpret_cast<uint16_t*>(B2 + q * C::B2_PART + off) = pt[q];
+    }
+    // two-level twiddles: W_N^e for e < 64, then W_N^(64 h) for h < 64
+    for (int e = tid; e < 128; e += 128) {
+        const int j = e < 64 ? e : (e - 64) * 64;
+        double sn, cs;
+        sincospi(2.0 * (double)(j % N) / (double)N, &sn, &cs);
+        TWL[e] = make_float2((float)cs, (float)(-sn));
+    }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t d1 = tmem, d2 = tmem + C::NO1;
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    constexpr uint32_t ID1 = idesc_pm<PM>(128, C::NO1);
+    constexpr uint32_t ID2 = idesc_pm<PM>(128, C::NO2);
+    constexpr int NPROD = PARTS == 3 ? 6 : 3;
+    constexpr int PA[6] = {0, 0, 1, 0, 2, 1};
+    constexpr int PB[6] = {0, 1, 0, 2, 0, 1};
+    const uint32_t sa = smem_u32(A), sb1 = smem_u32(B1), sb2 = smem_u32(B2);
+
+    const uint64_t ntiles = (a.frames + FPT - 1) / FPT;
+    uint32_t phase = 0;
+    bool aborted = false;
+    for (uint64_t tile = blockIdx.x; tile < ntiles && !aborted; tile += gridDim.x) {
+        const uint64_t f0 = tile * FPT;
+        // ---------------- load + window + DC + scale + split -> A1 (one warp per frame)
+        for (int lf = warp; lf < FPT; lf += 4) {
+            const uint64_t f = f0 + lf;
+            const bool act = f < a.frames;
+            const uint64_t s0 = f * a.hop;
+            // first read: sum, minimum and maximum of the windowed frame
+            float sum = 0.0f, mn = 0.0f, mx = 0.0f;
+            for (int j = 0; j < N / 256; ++j) {  // lane owns samples [8c, 8c+8), c = lane + 32 j
+                const int c = lane + 32 * j;
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const int i = 8 * c + q;
+                    const uint64_t gi = s0 + i;
+                    float v = (act && gi < a.n) ? a.x[gi] : 0.0f;
+                    if (a.win) v *= a.win[i];
+                    sum += v;
+                    mn = fminf(mn, v);
+                    mx = fmaxf(mx, v);
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                sum += __shfl_xor_sync(0xffffffffu, sum, o);
+                mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+                mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            }
+            const float mean = a.remove_dc ? sum * (1.0f / (float)N) : 0.0f;
+            const float peak = fmaxf(mx - mean, mean - mn);
+            int e2 = 0;
+            if (peak > 0.0f) frexpf(peak, &e2);  // peak in [2^(e2-1), 2^e2)
+            const float sc = ldexpf(1.0f, 14 - e2);
+            if (lane == 0) fscale[lf] = ldexpf(1.0f, e2 - 14);
+            // second read (through L1): centre, scale, split
+            for (int j = 0; j < N / 256; ++j) {
+                const int c = lane + 32 * j;
+                float v[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const int i = 8 * c + q;
+                    const uint64_t gi = s0 + i;
+                    float x = (act && gi < a.n) ? a.x[gi] : 0.0f;
+                    if (a.win) x *= a.win[i];
+                    v[q] = (x - mean) * sc;
+                }
+                uint4 pp[PARTS];
+                S::split8(v, pp);
+                // samples 8c .. 8c+7 = (g0 .. g0+7, m) with g = i mod Q, m = i / Q
+                const int i0 = 8 * c, m = i0 / Q, g0 = i0 % Q;
+                const uint32_t off = mn_off(lf * Q + g0, m);
+#pragma unroll
+                for (int k = 0; k < PARTS; ++k) *reinterpret_cast<uint4*>(A + k * C::A1_PART + off) = pp[k];
+            }
+        }
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+        fence_after();
+        // ---------------- pass 1 on the tensor cores
+        if (tid == 0) {
+#pragma unroll
+            for (int ks = 0; ks < C::K1 / 16; ++ks) {
+#pragma unroll
+                for (int pr = 0; pr < NPROD; ++pr) {
+                    const uint64_t ad = sdesc(sa + PA[pr] * C::A1_PART + ks * 4096, 1024, 2048);
+                    const uint64_t bd = sdesc(sb1 + PB[pr] * C::B1_PART + ks * 32, 16, 1024);
+                    mma_f16(d1, ad, bd, ID1, (ks > 0 || pr > 0) ? 1u : 0u);
+                }
+            }
+            mma_commit(&mbar[0]);
+        }
+        if (!mbar_wait(&mbar[0], phase)) {
+            if (lane == 0) atomicExch(abort_flag, 1);
+        }
+        __syncthreads();
+        if (*abort_flag) {
+            aborted = true;
+            break;
+        }
+        fence_after();
+        // ---------------- epilogue 1: twiddle, scale by 1/P, split -> A2 (row = this thread)
+        {
+            const int lf = tid / Q, g = tid % Q;
+            constexpr float inv_p = 1.0f / (float)P;
+#pragma unroll 1
+            for (int k1b = 0; k1b < P; k1b += 8) {
+                float t[16];
+                tmem_ld16(d1 + lane_base + 2 * k1b, t);
+                float re[8], im[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const int e = (g * (k1b + q)) & (N - 1);
+                    const float2 w = cmul2(TWL[e & 63], TWL[64 + (e >> 6)]);
+                    const float yr = t[2 * q], yi = t[2 * q + 1];
+                    re[q] = (yr * w.x - yi * w.y) * inv_p;
+                    im[q] = (yr * w.y + yi * w.x) * inv_p;
+                }
+                uint4 pr_[PARTS], pi_[PARTS];
+                S::split8(re, pr_);
+                S::split8(im, pi_);
+                const int row2 = lf * P + k1b;  // 8 consecutive pass-2 rows, one block
+                unsigned char* blk = A + (row2 >> 7) * C::A2_BLOCK;
+                const uint32_t or_ = mn_off(row2 & 127, g), oi_ = mn_off(row2 & 127, Q + g);
+#pragma unroll
+                for (int k = 0; k < PARTS; ++k) {
+                    *reinterpret_cast<uint4*>(blk + k * C::A2_PART + or_) = pr_[k];
+                    *reinterpret_cast<uint4*>(blk + k * C::A2_PART + oi_) = pi_[k];
+                }
+            }
+        }
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+        fence_after();
+        // ---------------- pass 2 on the tensor cores, one MMA chain per 128-row block
+        if (tid == 0) {
+#pragma unroll
+            for (int b = 0; b < MB; ++b) {
+#pragma unroll
+                for (int ks = 0; ks < C::K2 / 16; ++ks) {
+#pragma unroll
+                    for (int pr = 0; pr < NPROD; ++pr) {
+                        const uint64_t ad =
+                            sdesc(sa + b * C::A2_BLOCK + PA[pr] * C::A2_PART + ks * 4096, 1024, 2048);
+                        const uint64_t bd =
+                            sdesc(sb2 + PB[pr] * C::B2_PART + (ks >> 2) * C::B2_PANEL + (ks & 3) * 32, 16, 1024);
+                        mma_f16(d2 + b * C::NO2, ad, bd, ID2, (ks > 0 || pr > 0) ? 1u : 0u);
+                    }
+                }
+            }
+            mma_commit(&mbar[1]);
+        }
+        if (!mbar_wait(&mbar[1], phase)) {
+            if (lane == 0) atomicExch(abort_flag, 1);
+        }
+        __syncthreads();
+        if (*abort_flag) {
+            aborted = true;
+            break;
+        }
+        fence_after();
+        // ---------------- epilogue 2: thread = (frame, k1) of each block holds X[k1 + P k2]
+#pragma unroll 1
+        for (int b = 0; b < MB; ++b) {
+            const int row2 = b * 128 + tid, lf = row2 / P, k1 = row2 % P;
+            const uint64_t f = f0 + lf;
+            const bool act = f < a.frames;
+            const float back = fscale[lf] * (float)P;  // undo both scalings (powers of two)
+#pragma unroll 1
+            for (int k2b = 0; k2b < Q; k2b += 8) {
+                float t[16];
+                tmem_ld16(d2 + b * C::NO2 + lane_base + 2 * k2b, t);
+                if (!act) continue;
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const int k = k1 + P * (k2b + q);
+                    const float xr = t[2 * q] * back, xi = t[2 * q + 1] * back;
+                    if constexpr (OUTK == OUT_HALF) {
+                        float2* o2 = reinterpret_cast<float2*>(a.out);
+                        const float2 X = make_float2(xr, xi);
+                        if (!a.dense) {
+                            const uint64_t flat = f * (uint64_t)N + k;
+                            if (flat < a.ohalf) __stcs(o2 + flat, X);
+                        } else if (k <= N / 2) {
+                            __stcs(o2 + f * (uint64_t)(N / 2 + 1) + k, X);
+                        }
+                    } else {
+                        if (k > N / 2) continue;
+                        const float p = (OUTK == OUT_POWER_SERIAL) ? fabsf(xr) * 1.41421356237309505f
+                                                                   : sqrtf(xr * xr + xi * xi);
+                        if (!a.dense) {
+                            float* rowp = a.out + f * (uint64_t)N;
+                            __stcs(rowp + k, p);
+                            if (k != 0 && k != N / 2) __stcs(rowp + (N - k), p);
+                        } else {
+                            __stcs(a.out + f * (uint64_t)(N / 2 + 1) + k, p);
+                        }
+                    }
+                }
+            }
+        }
+        fence_before();
+        __syncthreads();
+        fence_after();
+        phase ^= 1u;
+    }
+    // ---------------- release tensor memory (every exit path)
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 0) {
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(C::TMEM_COLS));
+    }
+    if (aborted && tid == 0) *reinterpret_cast<volatile int*>(err) = 1;
+}
+
+template <int P, int Q, int OUTK, int PM>
+cudaError_t launch_tcg_t(const FusedArgs& a, int* err, int sms, cudaStream_t st)
+{
+    using C = TcgCfg<P, Q, PM>;
+    if constexpr (!C::FITS) {
+        return cudaErrorInvalidValue;
+    } else {
+        auto k = stft_tcg_kernel<P, Q, OUTK, PM>;
+        static int per_sm = 0;
+        if (!per_sm) {
+            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM);
+            if (e != cudaSuccess) return e;
+            int occ = 0;
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 128, C::SMEM);
+            if (e != cudaSuccess) return e;
+            // CTAs resident on one SM must also fit its 512 tensor-memory columns
+            const int by_tmem = 512 / (int)C::TMEM_COLS;
+            per_sm = occ < 1 ? 1 : (occ < by_tmem ? occ : by_tmem);
+        }
+        const uint64_t ntiles = (a.frames + C::FPT - 1) / C::FPT;
+        const uint64_t cap = (uint64_t)sms * per_sm;
+        const uint64_t grid = ntiles < cap ? ntiles : cap;
+        k<<<(unsigned)(grid ? grid : 1), 128, C::SMEM, st>>>(a, err);
+        return cudaGetLastError();
+    }
+}
+
+template <int P, int Q, int PM>
+cudaError_t launch_tcg_o(int outk, const FusedArgs& a, int* err, int sms, cudaStream_t st)
+{
+    if (outk == OUT_HALF) return launch_tcg_t<P, Q, OUT_HALF, PM>(a, err, sms, st);
+    if (outk == OUT_POWER_SERIAL) return launch_tcg_t<P, Q, OUT_POWER_SERIAL, PM>(a, err, sms, st);
+    return launch_tcg_t<P, Q, OUT_POWER, PM>(a, err, sms, st);
+}
+
+template <int P, int Q>
+cudaError_t launch_tcg_p(int pm, int outk, const FusedArgs& a, int* err, int sms, cudaStream_t st)
+{
+    if (pm == PM_BF16X2) return launch_tcg_o<P, Q, PM_BF16X2>(outk, a, err, sms, st);
+    if (pm == PM_BF16X3) return launch_tcg_o<P, Q, PM_BF16X3>(outk, a, err, sms, st);
+    return launch_tcg_o<P, Q, PM_FP16X2>(outk, a, err, sms, st);
+}
+
 template <int R, int PM>
 const unsigned char* tc_tables(cudaError_t* e)
 {
@@ -1155,9 +1527,19 @@ cudaError_t launch_tc_t(const FusedArgs& a, int* err, int sms, cudaStream_t st)
 
 }  // namespace
 
-bool tc_supports(int exp) { return exp == 8 || exp == 10; }
+bool tc_supports(int exp) { return exp >= 8 && exp <= 12; }
 
-bool tc_piped(int exp, uint64_t hop) { return hop <= (1ull << exp); }
+bool tc_mode_supported(int exp, int pm)
+{
+    if (!tc_supports(exp)) return false;
+    // the generic form's bf16 hi/mid/lo operands at 4096 exceed shared memory
+    return !(exp == 12 && pm == PM_BF16X3);
+}
+
+// whether every split mode is available for this frame advance: the
+// pipelined forms (windows 2^8 and 2^10) stage a span sized for hop <= N;
+// the generic form (2^9, 2^11, 2^12) takes any advance
+bool tc_piped(int exp, uint64_t hop) { return (exp != 8 && exp != 10) || hop <= (1ull << exp); }
 
 cudaError_t launch_tc(int exp, int outk, int pm, const FusedArgs& a, int* err, int test_stall, int sms,
                       cudaStream_t st)
@@ -1167,6 +1549,9 @@ cudaError_t launch_tc(int exp, int outk, int pm, const FusedArgs& a, int* err, i
     const bool piped = tc_piped(exp, a.hop) && (reinterpret_cast<uintptr_t>(a.x) & 3u) == 0;
     if (piped && exp == 8) return launch_tc2_p<16>(pm, outk, a, err, test_stall, sms, st);
     if (piped && exp == 10) return launch_tc2_p<32>(pm, outk, a, err, test_stall, sms, st);
+    if (exp == 9) return launch_tcg_p<32, 16>(pm, outk, a, err, sms, st);
+    if (exp == 11) return launch_tcg_p<64, 32>(pm, outk, a, err, sms, st);
+    if (exp == 12) return launch_tcg_p<64, 64>(pm, outk, a, err, sms, st);
     if (pm != PM_FP16X2) return cudaErrorInvalidValue;
     if (exp == 8) {
         if (outk == OUT_HALF) return launch_tc_t<16, OUT_HALF>(a, err, sms, st);

@@ -1,8 +1,10 @@
-"""Tensor-core split-precision form (tcgen05): windows 2^8 and 2^10, every
-output layout, against the FP64 oracle.  fp16 hi/lo (--precision=tc-fp16) and
-bf16 hi/mid/lo (tc-bf16x3) meet the suite's relative-L2 bar of 1e-5; bf16
-hi/lo (tc-bf16x2, about 16 significant bits per operand) is reported for
-reference and held to 1e-4."""
+"""Tensor-core split-precision form (tcgen05): windows 2^8 .. 2^12 (the
+pipelined kernel at 2^8 and 2^10, the generic N = P x Q kernel at 2^9, 2^11
+and 2^12), every output layout, against the FP64 oracle.  fp16 hi/lo
+(--precision=tc-fp16) and bf16 hi/mid/lo (tc-bf16x3) meet the suite's
+relative-L2 bar of 1e-5; bf16 hi/lo (tc-bf16x2, about 16 significant bits per
+operand) is reported for reference and held to 1e-4.  bf16 hi/mid/lo at 2^12
+does not fit shared memory and is refused."""
 import numpy as np
 import pytest
 
@@ -12,7 +14,7 @@ REL_L2 = 1e-5
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("exp", [8, 10])
+@pytest.mark.parametrize("exp", [8, 9, 10, 11, 12])
 @pytest.mark.parametrize("opts", [
     "--hanning_window",
     "--hanning_window --remove_dc --half_complex_return",
@@ -32,23 +34,26 @@ def test_tc_matches_fp64(ocs_lib, orc, exp, opts):
         assert err <= REL_L2, (exp, ov, opts, err)
 
 
-def test_tc_scaling_extremes(ocs_lib, orc):
+@pytest.mark.parametrize("exp", [10, 11, 12])
+def test_tc_scaling_extremes(ocs_lib, orc, exp):
     """Per-frame power-of-two scaling keeps fp16 in range for tiny and huge signals."""
     for amp in (1e-6, 1.0, 3e4):
         x = (signal(5, 50000) * amp).astype(np.float32)
-        got = ocs_lib.activate(x, 10, 0.75, "--hanning_window --precision=tc-fp16")
-        ref = orc.fp64_stft(x, 10, 0.75, "--hanning_window")
-        assert orc.rel_l2(got, ref) <= REL_L2, amp
+        got = ocs_lib.activate(x, exp, 0.75, "--hanning_window --precision=tc-fp16")
+        ref = orc.fp64_stft(x, exp, 0.75, "--hanning_window")
+        assert orc.rel_l2(got, ref) <= REL_L2, (exp, amp)
 
 
 @pytest.mark.parametrize("prec,bar", [("tc-bf16x3", 1e-5), ("tc-bf16x2", 1e-4)])
-@pytest.mark.parametrize("exp", [8, 10])
+@pytest.mark.parametrize("exp", [8, 9, 10, 11, 12])
 @pytest.mark.parametrize("opts", [
     "--hanning_window --remove_dc",
     "--blackman_window --half_complex_return --layout=dense",
     "--hamming_window --half_complex_return",
 ])
 def test_tc_bf16_modes(ocs_lib, orc, prec, bar, exp, opts):
+    if exp == 12 and prec == "tc-bf16x3":
+        pytest.skip("not available at 2^12 (test_tc_bf16x3_refused_at_4096)")
     N = 1 << exp
     x = signal(300 + exp, 900 * N + 77)  # many tiles per CTA
     for ov in (0.75, 0.3):
@@ -64,11 +69,27 @@ def test_tc_bf16_needs_short_advance(ocs_lib):
 
 
 def test_tc_rejects_unsupported_window(ocs_lib):
-    with pytest.raises(ocs_lib.OcsError):
-        ocs_lib.activate(signal(1, 10000), 9, 0.5, "--precision=tc-fp16")
+    for exp in (7, 13):
+        with pytest.raises(ocs_lib.OcsError):
+            ocs_lib.activate(signal(1, 10000), exp, 0.5, "--precision=tc-fp16")
 
 
-@pytest.mark.parametrize("exp", [8, 10])
+def test_tc_bf16x3_refused_at_4096(ocs_lib):
+    with pytest.raises(ocs_lib.OcsError, match="does not fit"):
+        ocs_lib.activate(signal(1, 50000), 12, 0.5, "--precision=tc-bf16x3")
+
+
+@pytest.mark.parametrize("exp", [9, 11, 12])
+def test_tc_generic_any_advance(ocs_lib, orc, exp):
+    """The generic kernel takes frame advances above the window in every mode."""
+    x = signal(40 + exp, 200_003)
+    for prec, bar in (("tc-fp16", REL_L2), ("tc-bf16x2", 1e-4)):
+        got = ocs_lib.activate(x, exp, -0.5, "--hanning_window --precision=" + prec)
+        ref = orc.fp64_stft(x, exp, -0.5, "--hanning_window")
+        assert orc.rel_l2(got, ref) <= bar, (exp, prec)
+
+
+@pytest.mark.parametrize("exp", [8, 9, 10, 11, 12])
 def test_tc_many_tiles_per_cta(ocs_lib, orc, exp):
     """Long signals: every CTA runs many tiles, so each double buffer is
     reused many times (phase parity of every pipeline barrier wraps)."""
@@ -100,7 +121,7 @@ def test_tc_hop_longer_than_window(ocs_lib, orc):
     """Negative overlap (frame advance above the window) takes the
     non-pipelined tensor-core kernel."""
     x = signal(8, 100_000)
-    for exp in (8, 10):
+    for exp in (8, 9, 10, 11, 12):
         got = ocs_lib.activate(x, exp, -0.5, "--hanning_window --precision=tc-fp16")
         ref = orc.fp64_stft(x, exp, -0.5, "--hanning_window")
         assert orc.rel_l2(got, ref) <= REL_L2, exp
@@ -142,7 +163,7 @@ def test_tc_wait_timeout_reports_error():
     assert after <= REL_L2
 
 
-@pytest.mark.parametrize("exp,ov", [(8, 0.3), (10, 0.33), (10, 0.1), (8, 0.0)])
+@pytest.mark.parametrize("exp,ov", [(8, 0.3), (10, 0.33), (10, 0.1), (8, 0.0), (9, 0.3), (11, 0.1), (12, 0.33)])
 def test_tc_odd_hop(ocs_lib, orc, exp, ov):
     """Frame advances that are not a multiple of four samples: frames start
     at every offset inside a 16-byte word of the staged input."""
