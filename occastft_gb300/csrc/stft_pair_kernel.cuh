@@ -63,13 +63,21 @@ __host__ __device__ constexpr int pair_smem_tw_entries(int exp)
     return pair_tables_in_smem(exp) ? pair_tw_size(exp)
                                     : (pair_cfg(exp).nstages > 2 ? pair_tw_offset(exp, 2) : pair_tw_size(exp));
 }
-// The window joins them except at 2^13: there its 32 KB would leave L1 too
-// small for the second stage's 57 KB of twiddles (measured 258 -> 240
-// Gsamples/s with it, and no better with the largest shared carveout).
+// The window joins them except at 2^13, where its 32 KB would take from L1
+// what the overlapping frames' loads reuse (2^13 power: 278 Gsamples/s with
+// the window read through L1, 254 with it in shared memory).
 __host__ __device__ constexpr bool pair_smem_window(int exp) { return exp != 13; }
+// From 2^12 the later stages' twiddles come from a two-level table in shared
+// memory, W_N^e = lo[e & 127] * hi[e >> 7] (128 + N/128 entries), chained
+// between sparse lookups as in the one-frame kernels, instead of the plan
+// table through L1 (at 2^14 that table is 123 KB and misses L1): 2^12 276 ->
+// 280, 2^13 268 -> 278, 2^14 211 -> 218 Gsamples/s (power).
+__host__ __device__ constexpr bool pair_tw2l(int exp) { return exp >= 12; }
+__host__ __device__ constexpr size_t pair_tw2l_bytes(int exp) { return pair_tw2l(exp) ? (128 + (1 << exp) / 128) * 8 : 0; }
 __host__ __device__ constexpr size_t pair_tab_bytes(int exp)
 {
-    return (size_t)pair_smem_tw_entries(exp) * 8 + (pair_smem_window(exp) ? (size_t)(1 << exp) * 4 : 0);
+    return (size_t)pair_smem_tw_entries(exp) * 8 + pair_tw2l_bytes(exp) +
+           (pair_smem_window(exp) ? (size_t)(1 << exp) * 4 : 0);
 }
 __host__ __device__ constexpr size_t pair_smem_bytes_ct(int exp)
 {
@@ -131,9 +139,10 @@ struct PairCore {
     }
 
     // tws: shared-memory copy of the first pair_smem_tw_entries(EXP) twiddles;
-    // twg: the whole table in global memory (same indexing)
+    // twg: the whole table in global memory (same indexing); tw2: the
+    // two-level table (pair_tw2l) that replaces twg
     static __device__ __forceinline__ void fft(float2 (&v)[R], float2* buf, const float2* tws, const float2* twg,
-                                               int t)
+                                               const TwTwoLevel& tw2, int t)
     {
         {
             constexpr int r = C.radix[0];
@@ -163,13 +172,30 @@ struct PairCore {
             group_sync<T>();
 #pragma unroll
             for (int u = 0; u < R; ++u) v[u] = buf[pd(t + u * T)];
+            constexpr bool in_smem = pair_tw_offset(EXP, s + 1) <= pair_smem_tw_entries(EXP);
+            constexpr int ef = N / (ns * r);  // W_{ns r}^{j m} = W_N^{j m ef}
             static_for<0, R / r>([&](auto qc) {
                 constexpr int q = decltype(qc)::value;
                 const int j = (t + q * T) % ns;
-                static_for<1, r>([&](auto mc) {
-                    constexpr int m = decltype(mc)::value;
-                    v[q + m * (R / r)] = cmul(v[q + m * (R / r)], tw[toff + (m - 1) * ns + j]);
-                });
+                if constexpr (!in_smem && pair_tw2l(EXP)) {
+                    // a two-level lookup every 8th m, products with W^{j ef} between
+                    float2 b = make_float2(1.0f, 0.0f), w = b;
+                    static_for<1, r>([&](auto mc) {
+                        constexpr int m = decltype(mc)::value;
+                        if constexpr ((m - 1) % 8 == 0) {
+                            w = tw_get(tw2, 0, j * m * ef);
+                            if constexpr (m == 1) b = w;
+                        } else {
+                            w = cmul(w, b);
+                        }
+                        v[q + m * (R / r)] = cmul(v[q + m * (R / r)], w);
+                    });
+                } else {
+                    static_for<1, r>([&](auto mc) {
+                        constexpr int m = decltype(mc)::value;
+                        v[q + m * (R / r)] = cmul(v[q + m * (R / r)], tw[toff + (m - 1) * ns + j]);
+                    });
+                }
                 dft_inreg<R, r, q, R / r>(v);
             });
         });
@@ -206,13 +232,25 @@ struct PairCore {
 };
 
 template <int EXP>
-__device__ __forceinline__ void pair_tables(const FusedArgs& a, float2* s_tab, int tid, const float*& win)
+__device__ __forceinline__ void pair_tables(const FusedArgs& a, float2* s_tab, int tid, const float*& win,
+                                            TwTwoLevel& tw2)
 {
     constexpr int TWN = pair_smem_tw_entries(EXP);
     constexpr int N = 1 << EXP;
     for (int i = tid; i < TWN; i += blockDim.x) s_tab[i] = a.tw[i];
+    float2* s2 = s_tab + TWN;
+    if constexpr (pair_tw2l(EXP)) {
+        // lo[e] = W_N^e (e < 128), hi[h] = W_N^(128 h) (h < N / 128)
+        for (int i = tid; i < 128 + N / 128; i += blockDim.x) {
+            const int e = i < 128 ? i : (i - 128) * 128;
+            double sn, cs;
+            sincospi(2.0 * (double)e / (double)N, &sn, &cs);
+            s2[i] = make_float2((float)cs, (float)(-sn));
+        }
+        tw2 = TwTwoLevel{s2, s2 + 128};
+    }
     if constexpr (pair_smem_window(EXP)) {
-        float* sw = reinterpret_cast<float*>(s_tab + TWN);
+        float* sw = reinterpret_cast<float*>(reinterpret_cast<char*>(s2) + pair_tw2l_bytes(EXP));
         for (int i = tid; i < N; i += blockDim.x) sw[i] = a.win[i];
         win = sw;
     } else {
@@ -239,7 +277,8 @@ stft_pair_kernel(const FusedArgs a)
     float2* s_tab = smem + PPC * BS;
     float2* red = reinterpret_cast<float2*>(reinterpret_cast<char*>(s_tab) + pair_tab_bytes(EXP));
     const float* win;
-    pair_tables<EXP>(a, s_tab, tid, win);
+    TwTwoLevel tw2{nullptr, nullptr};
+    pair_tables<EXP>(a, s_tab, tid, win, tw2);
 
     const uint64_t pairs = (a.frames + 1) / 2;
     for (uint64_t pbase = (uint64_t)blockIdx.x * PPC; pbase < pairs; pbase += (uint64_t)gridDim.x * PPC) {
@@ -278,7 +317,7 @@ stft_pair_kernel(const FusedArgs a)
             }
         }
         if (a.remove_dc) K::remove_dc(v, red, tid, lp);
-        K::fft(v, buf, s_tab, a.tw, t);
+        K::fft(v, buf, s_tab, a.tw, tw2, t);
         K::partners_prepare(v, buf, t);
         const int src = K::partner_lane(tid, t);
 
