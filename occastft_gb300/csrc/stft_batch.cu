@@ -79,6 +79,20 @@ __device__ __forceinline__ void batch_tile(const FusedArgs& a, uint64_t f0, uint
     }
     FusedArgs b = a;
     b.frames = f0 + nf;  // frames past the tile belong to the next tile
+    // The output kind is the same for the whole tile.  Power tiles get a body
+    // specialised for it, except at 2^11 and 2^13, where the extra body makes
+    // the kernel spill under its 128-register cap (2^11 tiles fell from 0.49
+    // to 0.31 of HBM); other kinds take the run-time body.
+    auto run = [&](const auto& twx) {
+        if (EXP != 11 && EXP != 13 && a.outk == OUT_POWER) {
+            for (uint64_t fb = f0; fb < f0 + nf; fb += FPC)
+                fused_group_frames<EXP, (EXP != 11 && EXP != 13) ? OUT_POWER : OUT_RUNTIME>(b, fb, buf, red, twx,
+                                                                                             win2, tid, lf, t);
+        } else {
+            for (uint64_t fb = f0; fb < f0 + nf; fb += FPC)
+                fused_group_frames<EXP, OUT_RUNTIME>(b, fb, buf, red, twx, win2, tid, lf, t);
+        }
+    };
     if constexpr (EXP > kBatchSmemTabMaxExp) {
         float2* st = reinterpret_cast<float2*>(reinterpret_cast<char*>(smem) + batch_frames_smem());
         if (*s_tw != a.tw || *s_win != nullptr) {
@@ -90,12 +104,9 @@ __device__ __forceinline__ void batch_tile(const FusedArgs& a, uint64_t f0, uint
                 *s_win = nullptr;  // marks the region as holding a two-level table
             }
         }
-        const TwTwoLevel tw2{st, st + 128};
-        for (uint64_t fb = f0; fb < f0 + nf; fb += FPC)
-            fused_group_frames<EXP, OUT_RUNTIME>(b, fb, buf, red, tw2, win2, tid, lf, t);
+        run(TwTwoLevel{st, st + 128});
     } else {
-        for (uint64_t fb = f0; fb < f0 + nf; fb += FPC)
-            fused_group_frames<EXP, OUT_RUNTIME>(b, fb, buf, red, tw, win2, tid, lf, t);
+        run(tw);
     }
 }
 
