@@ -57,19 +57,38 @@ __global__ void __launch_bounds__(kTileC * (fused_M(EXP1) / fused_cfg(EXP1).R))
     const uint64_t f = a.f0 + fl;
     const uint64_t s0 = f * a.hop;
 
-    // rows of 8 complex samples (16 floats, 64 bytes): lane pairs take one row
-    for (int e = tid; e < M1 * kTileC; e += blockDim.x) {
-        const int col = e % kTileC, m1 = e / kTileC;
-        const uint64_t m = c0 + col + M2 * (uint64_t)m1;  // complex index in the frame
-        const uint64_t i = 2 * m;                          // real sample index in the frame
-        const uint64_t g = s0 + i;
-        float xr = 0.0f, xi = 0.0f;
-        if (f < a.frames_total) {
-            if (g < a.n) xr = a.x[g];
-            if (g + 1 < a.n) xi = a.x[g + 1];
+    // rows of 8 complex samples (16 floats, 64 bytes)
+    const uint64_t N = 2 * (uint64_t)M1 * M2;
+    const bool whole = f < a.frames_total && s0 + N <= a.n && (a.hop & 3) == 0 &&
+                       (reinterpret_cast<uintptr_t>(a.x) & 15) == 0;
+    if (whole) {
+        // frame inside the signal and 16-byte aligned: four threads per row,
+        // a float4 (two complex samples) each; row m1 starts at real index
+        // 2 (c0 + M2 m1), a multiple of 16
+        const float* xf = a.x + s0;
+        for (int e = tid; e < M1 * 4; e += blockDim.x) {
+            const int m1 = e >> 2, q = e & 3;
+            const uint32_t i = 2u * ((uint32_t)c0 + (uint32_t)M2 * (uint32_t)m1) + 4u * (uint32_t)q;
+            const float4 xv = *reinterpret_cast<const float4*>(xf + i);
+            const float4 w = *reinterpret_cast<const float4*>(a.win + i);
+            sbuf[(2 * q) * BS + K::pd(m1)] = make_float2(xv.x * w.x, xv.y * w.y);
+            sbuf[(2 * q + 1) * BS + K::pd(m1)] = make_float2(xv.z * w.z, xv.w * w.w);
         }
-        const float2 w = *reinterpret_cast<const float2*>(a.win + i);
-        sbuf[col * BS + K::pd(m1)] = make_float2(xr * w.x, xi * w.y);
+    } else {
+        // lane pairs take one row, samples past the signal end read as zero
+        for (int e = tid; e < M1 * kTileC; e += blockDim.x) {
+            const int col = e % kTileC, m1 = e / kTileC;
+            const uint64_t m = c0 + col + M2 * (uint64_t)m1;  // complex index in the frame
+            const uint64_t i = 2 * m;                          // real sample index in the frame
+            const uint64_t g = s0 + i;
+            float xr = 0.0f, xi = 0.0f;
+            if (f < a.frames_total) {
+                if (g < a.n) xr = a.x[g];
+                if (g + 1 < a.n) xi = a.x[g + 1];
+            }
+            const float2 w = *reinterpret_cast<const float2*>(a.win + i);
+            sbuf[col * BS + K::pd(m1)] = make_float2(xr * w.x, xi * w.y);
+        }
     }
     __syncthreads();
     const int col = tid / T, t = tid % T;
@@ -79,17 +98,25 @@ __global__ void __launch_bounds__(kTileC * (fused_M(EXP1) / fused_cfg(EXP1).R))
     for (int u = 0; u < R; ++u) v[u] = buf[K::pd(t + u * T)];
     K::fft(v, buf, a.tw1, t);  // slot u holds column FFT bin k1 = t + u*T
     __syncthreads();
+    // W_M^{c k1}, k1 = t + u T: a two-level lookup at u = 0 and 8, then
+    // products with W_M^{c T} (at most 7 rounding steps)
     const uint64_t c = c0 + col;
+    const float2 step = tw2l(a.twm_lo, a.twm_hi, c * (uint64_t)T);
+    float2 w = make_float2(1.0f, 0.0f);
 #pragma unroll
     for (int u = 0; u < R; ++u) {
         const int k1 = t + u * T;
-        buf[K::pd(k1)] = cmul(v[u], tw2l(a.twm_lo, a.twm_hi, c * (uint64_t)k1));
+        w = (u % 8 == 0) ? tw2l(a.twm_lo, a.twm_hi, c * (uint64_t)k1) : cmul(w, step);
+        buf[K::pd(k1)] = cmul(v[u], w);
     }
     __syncthreads();
+    // Y row-major: row k1 holds this CTA's 8 columns at c0 (64 bytes), written
+    // as four float4 (two complex values) per row
     float2* y = a.scratch + fl * (uint64_t)M1 * M2;
-    for (int e = tid; e < M1 * kTileC; e += blockDim.x) {
-        const int cc = e % kTileC, k1 = e / kTileC;
-        y[(uint64_t)k1 * M2 + c0 + cc] = sbuf[cc * BS + K::pd(k1)];
+    for (int e = tid; e < M1 * 4; e += blockDim.x) {
+        const int k1 = e >> 2, q = e & 3;
+        const float2 lo = sbuf[(2 * q) * BS + K::pd(k1)], hi = sbuf[(2 * q + 1) * BS + K::pd(k1)];
+        *reinterpret_cast<float4*>(y + (uint64_t)k1 * M2 + c0 + 2 * q) = make_float4(lo.x, lo.y, hi.x, hi.y);
     }
 }
 
@@ -134,53 +161,57 @@ __global__ void __launch_bounds__(2 * kTileR * (fused_M(EXP2) / fused_cfg(EXP2).
     __syncthreads();
     if (f >= a.frames_total) return;
 
-    // outputs: lanes over the 8 rows of a slot group, then over k2
+    // outputs: lanes over the 8 rows of a slot group, then over k2.  Thread
+    // tid keeps slot (tid & 7) of each group (first the rows, then their
+    // mirrors) and steps k2 by 16, so everything that depends on the slot is
+    // formed once per group.
     const bool dc = a.remove_dc != 0;
-    for (int e = tid; e < 2 * kTileR * M2; e += blockDim.x) {
-        const int s = (e % kTileR) + kTileR * (e / (kTileR * M2));
-        const int k2 = (e / kTileR) % M2;
-        const uint64_t k1 = row_of(s);
+    const uint32_t m1 = (uint32_t)M1, m2 = (uint32_t)M2;
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
+        const int s = (tid & (kTileR - 1)) + kTileR * h;
+        const uint32_t k1 = (uint32_t)row_of(s);
         // partner Z[M - k]: row (M1 - k1) mod M1; column M2-1-k2, or (M2-k2) mod M2 for row 0
-        int ps, pk2;
-        if (k1 == 0) {
-            ps = s;
-            pk2 = (M2 - k2) & (M2 - 1);
-        } else if (k1 == M1 / 2) {
-            ps = s;
-            pk2 = M2 - 1 - k2;
-        } else {
-            ps = s < kTileR ? s + kTileR : s - kTileR;
-            pk2 = M2 - 1 - k2;
-        }
-        const float2 A = sbuf[s * BS + K::pd(k2)];
-        const float2 B = sbuf[ps * BS + K::pd(pk2)];
-        const uint64_t k = k1 + M1 * (uint64_t)k2;
-        float2 ev, wo;
-        K::untangle(A, B, tw2l(a.twn_lo, a.twn_hi, k), ev, wo);
-        float2 X0 = make_float2(ev.x + wo.x, ev.y + wo.y);        // X[k]
-        const float2 X1 = make_float2(ev.x - wo.x, ev.y - wo.y);  // X[k + M]
-        if (dc && k == 0) X0 = make_float2(0.0f, 0.0f);
-        if constexpr (OUTK == OUT_HALF) {
-            float2* o2 = reinterpret_cast<float2*>(a.out);
-            if (!a.dense) {
-                const uint64_t flat = f * N + k;
-                if (flat < a.ohalf) __stcs(o2 + flat, X0);
-                if (flat + M < a.ohalf) __stcs(o2 + flat + M, X1);
+        const int ps = (k1 == 0 || k1 == m1 / 2) ? s : (s < kTileR ? s + kTileR : s - kTileR);
+        const bool row0 = k1 == 0;
+        const float2* zs = sbuf + s * BS;
+        const float2* zp = sbuf + ps * BS;
+        // W_N^k for k = k1 + M1 k2: W_N^{k1} W_{2 M2}^{k2}; the second factor
+        // is the untangle table of the M2-point plan (its first M2 entries)
+        const float2 wk1 = tw2l(a.twn_lo, a.twn_hi, k1);
+        float* ro = a.out + f * N;
+        float* rod = a.out + f * (M + 1);
+        float2* o2 = reinterpret_cast<float2*>(a.out);
+#pragma unroll 2
+        for (uint32_t k2 = (uint32_t)tid / kTileR; k2 < m2; k2 += blockDim.x / kTileR) {
+            const uint32_t pk2 = row0 ? ((m2 - k2) & (m2 - 1)) : (m2 - 1 - k2);
+            const float2 A = zs[K::pd((int)k2)];
+            const float2 B = zp[K::pd((int)pk2)];
+            const uint32_t k = k1 + m1 * k2;
+            float2 ev, wo;
+            K::untangle(A, B, cmul(wk1, a.tw2[k2]), ev, wo);
+            float2 X0 = make_float2(ev.x + wo.x, ev.y + wo.y);        // X[k]
+            const float2 X1 = make_float2(ev.x - wo.x, ev.y - wo.y);  // X[k + M]
+            if (dc && k == 0) X0 = make_float2(0.0f, 0.0f);
+            if constexpr (OUTK == OUT_HALF) {
+                if (!a.dense) {
+                    const uint64_t flat = f * N + k;
+                    if (flat < a.ohalf) __stcs(o2 + flat, X0);
+                    if (flat + M < a.ohalf) __stcs(o2 + flat + M, X1);
+                } else {
+                    float2* rc = o2 + f * (M + 1);
+                    __stcs(rc + k, X0);
+                    if (k == 0) __stcs(rc + M, X1);
+                }
             } else {
-                float2* ro = o2 + f * (M + 1);
-                __stcs(ro + k, X0);
-                if (k == 0) __stcs(ro + M, X1);
-            }
-        } else {
-            const float p0 = power_of<OUTK>(X0), p1 = power_of<OUTK>(X1);
-            if (!a.dense) {
-                float* ro = a.out + f * N;
-                __stcs(ro + k, p0);
-                __stcs(ro + k + M, p1);
-            } else {
-                float* ro = a.out + f * (M + 1);
-                __stcs(ro + k, p0);
-                if (k == 0) __stcs(ro + M, p1);
+                const float p0 = power_of<OUTK>(X0), p1 = power_of<OUTK>(X1);
+                if (!a.dense) {
+                    __stcs(ro + k, p0);
+                    __stcs(ro + k + M, p1);
+                } else {
+                    __stcs(rod + k, p0);
+                    if (k == 0) __stcs(rod + M, p1);
+                }
             }
         }
     }
