@@ -31,6 +31,21 @@ namespace {
 constexpr int kTileC = 8;  // columns per column-pass CTA
 constexpr int kTileR = 8;  // rows (and as many mirror rows) per row-pass CTA
 
+// Column-pass buffer stride: = 4 (mod 8) float2, so that the staging rows
+// (four lanes per row of 8 columns, two columns each, 8 rows per warp) cover
+// every bank twice per warp access.
+__host__ __device__ constexpr int large_col_stride(int exp1)
+{
+    return fused_buf_stride(exp1) + ((4 - fused_buf_stride(exp1) % 8) + 8) % 8;
+}
+// Row-pass buffers: row r starts at r * large_row_stride + large_row_shift(r),
+// the stride a multiple of 16 float2 and the shift 0, 8, 4, 12, 2, 10, 6, 14
+// for r mod 8.  The four rows a warp transforms at window 2^8 (8 lanes per row
+// on 8 consecutive slots) then tile the 16 bank pairs twice, and so do the
+// output loop's reads of 8 rows at 4 consecutive columns.
+__host__ __device__ constexpr int large_row_stride(int exp2) { return (fused_buf_stride(exp2) + 14 + 15) / 16 * 16; }
+__device__ __forceinline__ int large_row_shift(int r) { return 8 * (r & 1) + 4 * ((r >> 1) & 1) + 2 * ((r >> 2) & 1); }
+
 __host__ __device__ constexpr int large_l1(int exp) { return exp / 2; }         // log2 M1
 __host__ __device__ constexpr int large_l2(int exp) { return exp - 1 - exp / 2; }  // log2 M2
 
@@ -47,7 +62,7 @@ __global__ void __launch_bounds__(kTileC * (fused_M(EXP1) / fused_cfg(EXP1).R))
 {
     using K = Core<EXP1>;
     constexpr int M1 = K::M, R = K::R, T = K::T;
-    constexpr int BS = fused_buf_stride(EXP1);
+    constexpr int BS = large_col_stride(EXP1);
     extern __shared__ float2 sbuf[];  // kTileC column buffers of BS slots
     const int tid = threadIdx.x;
     const uint64_t M2 = a.m2;
@@ -127,8 +142,8 @@ __global__ void __launch_bounds__(2 * kTileR * (fused_M(EXP2) / fused_cfg(EXP2).
 {
     using K = Core<EXP2>;
     constexpr int M2 = K::M, R = K::R, T = K::T;
-    constexpr int BS = fused_buf_stride(EXP2);
-    extern __shared__ float2 sbuf[];  // 2*kTileR row buffers of BS slots
+    constexpr int BS = large_row_stride(EXP2);
+    extern __shared__ float2 sbuf[];  // 2*kTileR row buffers (large_row_stride / large_row_shift)
     const int tid = threadIdx.x;
     const uint64_t M1 = a.m1;
     const uint64_t M = M1 * M2;
@@ -147,7 +162,7 @@ __global__ void __launch_bounds__(2 * kTileR * (fused_M(EXP2) / fused_cfg(EXP2).
     };
     const int rs = tid / T, t = tid % T;
     const float2* y = a.scratch + fl * M;
-    float2* buf = sbuf + rs * BS;
+    float2* buf = sbuf + rs * BS + large_row_shift(rs);
     {
         const float2* yr = y + row_of(rs) * M2;
         float2 v[R];
@@ -174,8 +189,8 @@ __global__ void __launch_bounds__(2 * kTileR * (fused_M(EXP2) / fused_cfg(EXP2).
         // partner Z[M - k]: row (M1 - k1) mod M1; column M2-1-k2, or (M2-k2) mod M2 for row 0
         const int ps = (k1 == 0 || k1 == m1 / 2) ? s : (s < kTileR ? s + kTileR : s - kTileR);
         const bool row0 = k1 == 0;
-        const float2* zs = sbuf + s * BS;
-        const float2* zp = sbuf + ps * BS;
+        const float2* zs = sbuf + s * BS + large_row_shift(s);
+        const float2* zp = sbuf + ps * BS + large_row_shift(ps);
         // W_N^k for k = k1 + M1 k2: W_N^{k1} W_{2 M2}^{k2}; the second factor
         // is the untangle table of the M2-point plan (its first M2 entries)
         const float2 wk1 = tw2l(a.twn_lo, a.twn_hi, k1);
@@ -234,7 +249,7 @@ template <int EXP1>
 cudaError_t launch_columns_t(const LargeArgs& a, uint64_t frames, cudaStream_t st)
 {
     constexpr int T = fused_M(EXP1) / fused_cfg(EXP1).R;
-    constexpr size_t smem = (size_t)kTileC * fused_buf_stride(EXP1) * sizeof(float2);
+    constexpr size_t smem = (size_t)kTileC * large_col_stride(EXP1) * sizeof(float2);
     auto k = large_columns_kernel<EXP1>;
     static bool attr = false;
     if (!attr) {
@@ -251,7 +266,7 @@ template <int EXP2, int OUTK>
 cudaError_t launch_rows_t(const LargeArgs& a, uint64_t frames, cudaStream_t st)
 {
     constexpr int T = fused_M(EXP2) / fused_cfg(EXP2).R;
-    constexpr size_t smem = (size_t)2 * kTileR * fused_buf_stride(EXP2) * sizeof(float2);
+    constexpr size_t smem = (size_t)2 * kTileR * large_row_stride(EXP2) * sizeof(float2);
     auto k = large_rows_kernel<EXP2, OUTK>;
     static bool attr = false;
     if (!attr) {
