@@ -31,12 +31,14 @@ namespace {
 constexpr int kTileC = 8;  // columns per column-pass CTA
 constexpr int kTileR = 8;  // rows (and as many mirror rows) per row-pass CTA
 
-// Column-pass buffer stride: = 4 (mod 8) float2, so that the staging rows
-// (four lanes per row of 8 columns, two columns each, 8 rows per warp) cover
-// every bank twice per warp access.
+// Column-pass buffer stride: = 2 (mod 8) float2.  An 8-byte shared access is
+// served per half-warp; in the staging loops a half-warp is 4 rows x 4 lanes,
+// lane q on columns 2q and 2q+1, so the columns must start 4 bank pairs
+// apart for the 16 lanes to hit 16 distinct ones (with = 4 (mod 8) lanes q
+// and q + 2 collided: 2.9 wavefronts per load where 2 are needed).
 __host__ __device__ constexpr int large_col_stride(int exp1)
 {
-    return fused_buf_stride(exp1) + ((4 - fused_buf_stride(exp1) % 8) + 8) % 8;
+    return fused_buf_stride(exp1) + ((2 - fused_buf_stride(exp1) % 8) + 8) % 8;
 }
 // Row-pass buffers: row r starts at r * large_row_stride + large_row_shift(r),
 // the stride a multiple of 16 float2 and the shift 0, 8, 4, 12, 2, 10, 6, 14
