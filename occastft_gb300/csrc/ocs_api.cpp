@@ -187,7 +187,8 @@ int get_window(int kind, int exp, float sigma, bool scaled, const float** out)
 // ---------------------------------------------------------------- kernel choice
 // Variants of the fused kernel: 0 one frame per FFT, direct I/O; 1 one frame
 // per FFT, shared-memory staged I/O (windows <= 2^9); 2 two frames per FFT;
-// 3 N/64 lanes per frame, the FFT in registers (windows 2^6 .. 2^8, power outputs).
+// 3 N/64 lanes per frame, the FFT in registers (windows 2^6 .. 2^8 for power,
+// 2^6 for half-complex).
 enum { VAR_DIRECT = 0, VAR_STAGED = 1, VAR_PAIR = 2, VAR_TPF = 3, VAR_COUNT = 4 };
 
 bool env_is(const char* name, const char* val)
@@ -206,7 +207,7 @@ int default_variant(int exp, int outk)
         if (exp == 9 || exp == 10 || exp == 12 || exp == 13 || exp == 14) return VAR_PAIR;
         return VAR_DIRECT;
     }
-    if (exp == 6) return VAR_STAGED;
+    if (exp == 6) return VAR_TPF;
     if (exp == 14) return VAR_PAIR;
     return VAR_DIRECT;
 }

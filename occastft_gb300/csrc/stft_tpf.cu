@@ -44,12 +44,76 @@ struct TpfCfg {
     static constexpr size_t SMEM = (size_t)N * 4 + (size_t)(kTpfThreads / 32) * 32 * RS * 4;
 };
 
+// Half-complex output of the lane's frame (Z[k] in v[k], k < M): the N
+// complex bins leave in two passes of M, each staged in the frame's row with a
+// stride of M + 1 complex values (so a half-warp's 8-byte stores hit 16
+// distinct bank pairs) and copied out 32 rows at a time.  Pass 0 holds bins
+// 0 .. M-1 (X[k], and X[M-k] = conj X[k+M]); pass 1 bins M .. N-1 (X[k+M], and
+// X[N-k] = conj X[k]); the dense layout (bins 0 .. M) takes pass 0 plus X[M].
+template <int N>
+__device__ __forceinline__ void tpf_half_out(const FusedArgs& a, const float2 (&v)[N / 2], float* rows,
+                                             uint64_t f0, int lane)
+{
+    constexpr int M = N / 2, OS = M + 1;  // output row stride in float2
+    float2* rows2 = reinterpret_cast<float2*>(rows);
+    float2* orow = rows2 + lane * OS;
+    float2* out2 = reinterpret_cast<float2*>(a.out);
+    const int nf = (a.frames - f0) < 32 ? (int)(a.frames - f0) : 32;
+    static_for<0, 2>([&](auto hc) {
+        constexpr int hf = decltype(hc)::value;
+        if (hf == 1 && a.dense) return;
+        static_for<0, M / 2 + 1>([&](auto kc) {
+            constexpr int k = decltype(kc)::value;
+            const float2 A = v[k];
+            const float2 B = v[(M - k) % M];
+            const float2 e = make_float2(A.x + B.x, A.y - B.y);
+            const float2 od = make_float2(A.y + B.y, B.x - A.x);
+            const float2 wo = twc<k, N>(od);
+            const float2 x0 = make_float2(e.x + wo.x, e.y + wo.y);  // X[k]
+            const float2 x1 = make_float2(e.x - wo.x, e.y - wo.y);  // X[k + M]
+            if constexpr (hf == 0) {
+                orow[k] = x0;
+                if constexpr (k != 0 && k != M / 2) orow[M - k] = make_float2(x1.x, -x1.y);
+                if constexpr (k == 0) {
+                    if (a.dense) orow[M] = x1;
+                }
+            } else {
+                orow[k] = x1;
+                if constexpr (k != 0 && k != M / 2) orow[M - k] = make_float2(x0.x, -x0.y);
+            }
+        });
+        __syncwarp();
+        if (!a.dense) {
+            // row jj, pass hf: bins hf M .. hf M + M - 1 of frame f0 + jj, flat index (f0 + jj) N + bin
+            const uint64_t base = f0 * (uint64_t)N + (uint64_t)hf * M;
+            if (nf == 32 && base + 31ull * N + M <= a.ohalf) {
+#pragma unroll 4
+                for (int jj = 0; jj < 32; ++jj)
+                    for (int c = lane; c < M; c += 32) __stcs(out2 + base + (uint64_t)jj * N + c, rows2[jj * OS + c]);
+            } else {
+                for (int jj = 0; jj < nf; ++jj)
+                    for (int c = lane; c < M; c += 32) {
+                        const uint64_t flat = base + (uint64_t)jj * N + c;
+                        if (flat < a.ohalf) __stcs(out2 + flat, rows2[jj * OS + c]);
+                    }
+            }
+        } else {
+            float2* dst = out2 + f0 * (uint64_t)(M + 1);
+            for (int t = lane; t < nf * (M + 1); t += 32) {
+                const int jj = t / (M + 1), c = t - jj * (M + 1);
+                __stcs(dst + t, rows2[jj * OS + c]);
+            }
+        }
+        __syncwarp();  // the rows take the next pass (or the next frames)
+    });
+}
+
 template <int EXP, int OUTK>
 __global__ void __launch_bounds__(kTpfThreads, 2) stft_tpf_kernel(const FusedArgs a)
 {
     using C = TpfCfg<EXP>;
     constexpr int N = C::N, M = C::M, RS = C::RS;
-    static_assert(OUTK == OUT_POWER || OUTK == OUT_POWER_SERIAL, "power outputs only");
+    static_assert(OUTK == OUT_POWER || OUTK == OUT_POWER_SERIAL || OUTK == OUT_HALF, "power or half-complex");
     extern __shared__ float4 smem4[];
     float* s_win = reinterpret_cast<float*>(smem4);  // N floats, window x 1/2
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -139,6 +203,11 @@ __global__ void __launch_bounds__(kTpfThreads, 2) stft_tpf_kernel(const FusedArg
         }
         dft_inreg<M, M, 0, 1>(v);  // Z[k] in slot k
         __syncwarp();              // every lane has read its row
+
+        if constexpr (OUTK == OUT_HALF) {
+            tpf_half_out<N>(a, v, rows, f0, lane);
+            continue;
+        }
 
         // ---------------- untangle, power, back into the row
         float o[OUTK == OUT_POWER || OUTK == OUT_POWER_SERIAL ? N : 1];
@@ -527,7 +596,11 @@ int occupancy_tpfl_t()
 
 }  // namespace
 
-bool tpf_has(int exp, int outk) { return exp >= 6 && exp <= 8 && (outk == OUT_POWER || outk == OUT_POWER_SERIAL); }
+bool tpf_has(int exp, int outk)
+{
+    if (outk == OUT_HALF) return exp == 6;
+    return exp >= 6 && exp <= 8 && (outk == OUT_POWER || outk == OUT_POWER_SERIAL);
+}
 int tpf_frames_per_cta(int exp)
 {
     if (exp == 7) return TplCfg<7>::THREADS / 32 * TplCfg<7>::F;
@@ -537,6 +610,7 @@ int tpf_frames_per_cta(int exp)
 
 cudaError_t launch_tpf(int exp, int outk, const FusedArgs& a, int grid, cudaStream_t st)
 {
+    if (outk == OUT_HALF) return exp == 6 ? launch_tpf_t<6, OUT_HALF>(a, grid, st) : cudaErrorInvalidValue;
     const bool ser = outk == OUT_POWER_SERIAL;
     if (outk != OUT_POWER && !ser) return cudaErrorInvalidValue;
     switch (exp) {
@@ -549,6 +623,7 @@ cudaError_t launch_tpf(int exp, int outk, const FusedArgs& a, int grid, cudaStre
 
 int tpf_occupancy(int exp, int outk)
 {
+    if (outk == OUT_HALF) return exp == 6 ? occupancy_tpf_t<6, OUT_HALF>() : 0;
     const bool ser = outk == OUT_POWER_SERIAL;
     if (outk != OUT_POWER && !ser) return 0;
     switch (exp) {

@@ -1,5 +1,5 @@
-"""The thread-per-frame kernels (power outputs; one lane per frame at window
-2^6, two and four lanes per frame at 2^7 and 2^8), forced with OCS_KERNEL=tpf,
+"""The thread-per-frame kernels (one lane per frame at window 2^6, power and
+half-complex; two and four lanes per frame at 2^7 and 2^8, power), forced with OCS_KERNEL=tpf,
 against the FP64 oracle: frame advances that are multiples of 4, 2 and 1
 samples (16-, 8- and 4-byte copies), ragged signal ends, one frame, DC
 removal, the dense layout and the Serial runner's power."""
@@ -23,7 +23,9 @@ def tpf(monkeypatch):
 def test_tpf_sizes_and_advances(tpf, ocs_lib, orc, exp, n, ov):
     x = signal(n % 1000 + 17, n)
     for opts in ("--hamming_window", "--hanning_window --remove_dc", "--blackman_window --layout=dense",
-                 "--flattop_window --serial_power", "--nuttall_window --remove_dc --layout=dense"):
+                 "--flattop_window --serial_power", "--nuttall_window --remove_dc --layout=dense",
+                 "--hamming_window --half_complex_return",
+                 "--blackman_window --remove_dc --half_complex_return --layout=dense"):
         got = ocs_lib.activate(x, exp, ov, opts)
         ref = orc.fp64_stft(x, exp, ov, opts)
         assert got.size == ref.size
