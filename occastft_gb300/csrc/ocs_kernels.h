@@ -78,6 +78,7 @@ struct LargeArgs {
     uint64_t hop;
     uint64_t f0;             // first frame of this launch (absolute)
     uint64_t frames_total;   // frames below this index are computed
+    uint64_t frames_launch;  // frames of this launch (set by launch_large)
     const float* win;        // window table scaled by 1/2 (N floats)
     float2* scratch;         // frames of this launch x M complex
     float* out;              // whole output

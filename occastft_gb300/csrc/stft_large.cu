@@ -58,82 +58,121 @@ __device__ __forceinline__ float2 tw2l(const float2* lo, const float2* hi, uint6
 }
 
 // ---------------------------------------------------------------- column pass
+// Column FFTs of up to 512 points (windows 2^16 .. 2^19) keep the CTA's
+// window coefficients in registers and take 4 consecutive frames of the same
+// columns per CTA; the larger ones (more chunks per thread, or 1024 threads
+// at 64 registers) take one frame per CTA and read the window each time.
+__host__ __device__ constexpr bool large_col_cache_win(int exp1)
+{
+    return (fused_M(exp1) * 4 / (8 * (fused_M(exp1) / fused_cfg(exp1).R))) <= 8 &&
+           8 * (fused_M(exp1) / fused_cfg(exp1).R) <= 256;
+}
+__host__ __device__ constexpr int large_col_frames(int exp1) { return large_col_cache_win(exp1) ? 4 : 1; }
+
 template <int EXP1>
 __global__ void __launch_bounds__(kTileC * (fused_M(EXP1) / fused_cfg(EXP1).R))
     large_columns_kernel(const LargeArgs a)
 {
     using K = Core<EXP1>;
     constexpr int M1 = K::M, R = K::R, T = K::T;
+    constexpr int NT = kTileC * T;      // threads
+    constexpr int NE = M1 * 4 / NT;     // float4 row chunks per thread (= R / 2)
     constexpr int BS = large_col_stride(EXP1);
     extern __shared__ float2 sbuf[];  // kTileC column buffers of BS slots
     const int tid = threadIdx.x;
     const uint64_t M2 = a.m2;
     const uint64_t tiles = M2 / kTileC;
-    const uint64_t fl = blockIdx.x / tiles;  // frame within this launch
+    const uint64_t fg = blockIdx.x / tiles;  // group of FPC frames within this launch
     const uint64_t c0 = (blockIdx.x % tiles) * kTileC;
-    const uint64_t f = a.f0 + fl;
-    const uint64_t s0 = f * a.hop;
-
-    // rows of 8 complex samples (16 floats, 64 bytes)
     const uint64_t N = 2 * (uint64_t)M1 * M2;
-    const bool whole = f < a.frames_total && s0 + N <= a.n && (a.hop & 3) == 0 &&
-                       (reinterpret_cast<uintptr_t>(a.x) & 15) == 0;
-    if (whole) {
-        // frame inside the signal and 16-byte aligned: four threads per row,
-        // a float4 (two complex samples) each; row m1 starts at real index
-        // 2 (c0 + M2 m1), a multiple of 16
-        const float* xf = a.x + s0;
-        for (int e = tid; e < M1 * 4; e += blockDim.x) {
-            const int m1 = e >> 2, q = e & 3;
-            const uint32_t i = 2u * ((uint32_t)c0 + (uint32_t)M2 * (uint32_t)m1) + 4u * (uint32_t)q;
-            const float4 xv = *reinterpret_cast<const float4*>(xf + i);
-            const float4 w = *reinterpret_cast<const float4*>(a.win + i);
-            sbuf[(2 * q) * BS + K::pd(m1)] = make_float2(xv.x * w.x, xv.y * w.y);
-            sbuf[(2 * q + 1) * BS + K::pd(m1)] = make_float2(xv.z * w.z, xv.w * w.w);
-        }
-    } else {
-        // lane pairs take one row, samples past the signal end read as zero
-        for (int e = tid; e < M1 * kTileC; e += blockDim.x) {
-            const int col = e % kTileC, m1 = e / kTileC;
-            const uint64_t m = c0 + col + M2 * (uint64_t)m1;  // complex index in the frame
-            const uint64_t i = 2 * m;                          // real sample index in the frame
-            const uint64_t g = s0 + i;
-            float xr = 0.0f, xi = 0.0f;
-            if (f < a.frames_total) {
-                if (g < a.n) xr = a.x[g];
-                if (g + 1 < a.n) xi = a.x[g + 1];
-            }
-            const float2 w = *reinterpret_cast<const float2*>(a.win + i);
-            sbuf[col * BS + K::pd(m1)] = make_float2(xr * w.x, xi * w.y);
+    const bool aligned = (a.hop & 3) == 0 && (reinterpret_cast<uintptr_t>(a.x) & 15) == 0;
+    // this CTA's window coefficients: chunk j is row m1 = e / 4, columns 2q,
+    // 2q+1 (q = e % 4) with e = tid + j NT; row m1 starts at real index
+    // 2 (c0 + M2 m1), a multiple of 16
+    constexpr bool CACHE_WIN = large_col_cache_win(EXP1);
+    constexpr int FPC = large_col_frames(EXP1);
+    float4 wv[CACHE_WIN ? NE : 1];
+    if constexpr (CACHE_WIN) {
+#pragma unroll
+        for (int j = 0; j < NE; ++j) {
+            const int e = tid + j * NT, m1 = e >> 2, q = e & 3;
+            wv[j] = *reinterpret_cast<const float4*>(a.win + 2u * ((uint32_t)c0 + (uint32_t)M2 * (uint32_t)m1) +
+                                                     4u * (uint32_t)q);
         }
     }
-    __syncthreads();
     const int col = tid / T, t = tid % T;
     float2* buf = sbuf + col * BS;
-    float2 v[R];
-#pragma unroll
-    for (int u = 0; u < R; ++u) v[u] = buf[K::pd(t + u * T)];
-    K::fft(v, buf, a.tw1, t);  // slot u holds column FFT bin k1 = t + u*T
-    __syncthreads();
-    // W_M^{c k1}, k1 = t + u T: a two-level lookup at u = 0 and 8, then
-    // products with W_M^{c T} (at most 7 rounding steps)
     const uint64_t c = c0 + col;
-    const float2 step = tw2l(a.twm_lo, a.twm_hi, c * (uint64_t)T);
-    float2 w = make_float2(1.0f, 0.0f);
+
+#pragma unroll 1
+    for (int ff = 0; ff < FPC; ++ff) {
+        const uint64_t fl = fg * FPC + ff;  // frame within this launch
+        if (fl >= a.frames_launch) break;
+        const uint64_t f = a.f0 + fl;
+        const uint64_t s0 = f * a.hop;
+        if (ff > 0) __syncthreads();  // the previous frame's reads of the buffers are over
+        // rows of 8 complex samples (16 floats, 64 bytes)
+        if (aligned && f < a.frames_total && s0 + N <= a.n) {
+            // frame inside the signal and 16-byte aligned: four threads per
+            // row, a float4 (two complex samples) each
+            const float* xf = a.x + s0;
+            auto chunk = [&](int e, const float4& w) {
+                const int m1 = e >> 2, q = e & 3;
+                const uint32_t i = 2u * ((uint32_t)c0 + (uint32_t)M2 * (uint32_t)m1) + 4u * (uint32_t)q;
+                const float4 xv = *reinterpret_cast<const float4*>(xf + i);
+                sbuf[(2 * q) * BS + K::pd(m1)] = make_float2(xv.x * w.x, xv.y * w.y);
+                sbuf[(2 * q + 1) * BS + K::pd(m1)] = make_float2(xv.z * w.z, xv.w * w.w);
+            };
+            if constexpr (CACHE_WIN) {
 #pragma unroll
-    for (int u = 0; u < R; ++u) {
-        const int k1 = t + u * T;
-        w = (u % 8 == 0) ? tw2l(a.twm_lo, a.twm_hi, c * (uint64_t)k1) : cmul(w, step);
-        buf[K::pd(k1)] = cmul(v[u], w);
-    }
-    __syncthreads();
-    // Y row-major: row k1 holds this CTA's 8 columns at c0 (64 bytes), written
-    // as four float4 (two complex values) per row
-    float2* y = a.scratch + fl * (uint64_t)M1 * M2;
-    for (int e = tid; e < M1 * 4; e += blockDim.x) {
-        const int k1 = e >> 2, q = e & 3;
-        const float2 lo = sbuf[(2 * q) * BS + K::pd(k1)], hi = sbuf[(2 * q + 1) * BS + K::pd(k1)];
-        *reinterpret_cast<float4*>(y + (uint64_t)k1 * M2 + c0 + 2 * q) = make_float4(lo.x, lo.y, hi.x, hi.y);
+                for (int j = 0; j < NE; ++j) chunk(tid + j * NT, wv[j]);
+            } else {
+                for (int e = tid; e < M1 * 4; e += NT) {
+                    const uint32_t i = 2u * ((uint32_t)c0 + (uint32_t)M2 * (uint32_t)(e >> 2)) + 4u * (uint32_t)(e & 3);
+                    chunk(e, *reinterpret_cast<const float4*>(a.win + i));
+                }
+            }
+        } else {
+            // lane pairs take one row, samples past the signal end read as zero
+            for (int e = tid; e < M1 * kTileC; e += NT) {
+                const int cc = e % kTileC, m1 = e / kTileC;
+                const uint64_t m = c0 + cc + M2 * (uint64_t)m1;  // complex index in the frame
+                const uint64_t i = 2 * m;                         // real sample index in the frame
+                const uint64_t g = s0 + i;
+                float xr = 0.0f, xi = 0.0f;
+                if (f < a.frames_total) {
+                    if (g < a.n) xr = a.x[g];
+                    if (g + 1 < a.n) xi = a.x[g + 1];
+                }
+                const float2 w = *reinterpret_cast<const float2*>(a.win + i);
+                sbuf[cc * BS + K::pd(m1)] = make_float2(xr * w.x, xi * w.y);
+            }
+        }
+        __syncthreads();
+        float2 v[R];
+#pragma unroll
+        for (int u = 0; u < R; ++u) v[u] = buf[K::pd(t + u * T)];
+        K::fft(v, buf, a.tw1, t);  // slot u holds column FFT bin k1 = t + u*T
+        __syncthreads();
+        // W_M^{c k1}, k1 = t + u T: a two-level lookup at u = 0 and 8, then
+        // products with W_M^{c T} (at most 7 rounding steps)
+        const float2 step = tw2l(a.twm_lo, a.twm_hi, c * (uint64_t)T);
+        float2 w = make_float2(1.0f, 0.0f);
+#pragma unroll
+        for (int u = 0; u < R; ++u) {
+            const int k1 = t + u * T;
+            w = (u % 8 == 0) ? tw2l(a.twm_lo, a.twm_hi, c * (uint64_t)k1) : cmul(w, step);
+            buf[K::pd(k1)] = cmul(v[u], w);
+        }
+        __syncthreads();
+        // Y row-major: row k1 holds this CTA's 8 columns at c0 (64 bytes),
+        // written as four float4 (two complex values) per row
+        float2* y = a.scratch + fl * (uint64_t)M1 * M2;
+        for (int e = tid; e < M1 * 4; e += NT) {
+            const int k1 = e >> 2, q = e & 3;
+            const float2 lo = sbuf[(2 * q) * BS + K::pd(k1)], hi = sbuf[(2 * q + 1) * BS + K::pd(k1)];
+            *reinterpret_cast<float4*>(y + (uint64_t)k1 * M2 + c0 + 2 * q) = make_float4(lo.x, lo.y, hi.x, hi.y);
+        }
     }
 }
 
@@ -259,8 +298,11 @@ cudaError_t launch_columns_t(const LargeArgs& a, uint64_t frames, cudaStream_t s
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    const uint64_t grid = frames * (a.m2 / kTileC);
-    k<<<(unsigned)grid, kTileC * T, smem, st>>>(a);
+    constexpr int FPC = large_col_frames(EXP1);
+    const uint64_t grid = (frames + FPC - 1) / FPC * (a.m2 / kTileC);
+    LargeArgs b = a;
+    b.frames_launch = frames;
+    k<<<(unsigned)grid, kTileC * T, smem, st>>>(b);
     return cudaGetLastError();
 }
 
