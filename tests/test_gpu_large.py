@@ -53,3 +53,17 @@ def test_large_matches_reference_serial(ocs_lib, orc):
     got = ocs_lib.activate(x, 16, 0.5, "--hanning_window --serial_power")
     ref = orc.serial_pipeline(x, 16, 0.5, "--hanning_window")
     assert orc.rel_l2(got, ref) <= REL_L2
+
+
+@pytest.mark.parametrize("exp", [16, 18])
+def test_large_small_scratch(ocs_lib, orc, monkeypatch, exp):
+    """A 1 MB scratch limit: each launch pair holds a few frames, so the
+    column pass's groups of four frames end part-way through a launch."""
+    monkeypatch.setenv("OCS_LARGE_SCRATCH_MB", "1")
+    N = 1 << exp
+    x = signal(950 + exp, 7 * N + 333)
+    for opts, ov in (("--hamming_window", 0.5), ("--blackman_window --half_complex_return", 0.75),
+                     ("--hanning_window --remove_dc", 0.3)):
+        got = ocs_lib.activate(x, exp, ov, opts)
+        assert orc.rel_l2(got, orc.fp64_stft(x, exp, ov, opts)) <= REL_L2, (exp, opts, ov)
+

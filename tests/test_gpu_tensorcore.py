@@ -100,11 +100,12 @@ def test_tc_many_tiles_per_cta(ocs_lib, orc, exp):
         assert orc.rel_l2(got, ref) <= REL_L2, (exp, opts)
 
 
+@pytest.mark.parametrize("exp", [10, 11])
 @pytest.mark.parametrize("shift", [1, 2, 3, 5])
-def test_tc_unaligned_device_input(ocs_lib, orc, shift):
+def test_tc_unaligned_device_input(ocs_lib, orc, exp, shift):
     """Signal pointers that are not 16-byte aligned (offset by whole floats)."""
     import torch
-    exp, ov, opts = 10, 0.75, "--hamming_window --remove_dc --layout=dense"
+    ov, opts = 0.75, "--hamming_window --remove_dc --layout=dense"
     x = signal(31 + shift, 200_003)
     g = ocs_lib.geometry(x.size, exp, ov, opts)
     buf = torch.zeros(x.size + 8, dtype=torch.float32, device="cuda")
