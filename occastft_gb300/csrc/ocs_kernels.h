@@ -1,10 +1,29 @@
 // Internal interface between the C-ABI host code and the CUDA kernels.
 #pragma once
+#include <atomic>
 #include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
 
 namespace ocs {
+
+// Raises Kernel's dynamic shared-memory limit to `bytes` on the current
+// device, once per (kernel, device): function attributes belong to a device,
+// so a runner re-initialised on another device sets them again.  Threads that
+// race on the first call both set it, which is harmless.
+template <auto Kernel>
+inline cudaError_t ensure_smem_attr(size_t bytes)
+{
+    static std::atomic<uint64_t> done{0};  // bit d: device d (d < 64) is set
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const uint64_t bit = dev >= 0 && dev < 64 ? (1ull << dev) : 0;
+    if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+    e = cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess && bit) done.fetch_or(bit, std::memory_order_acq_rel);
+    return e;
+}
 
 // output kinds of the fused kernel (compile-time specialisations)
 enum : int {

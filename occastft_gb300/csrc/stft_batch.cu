@@ -165,13 +165,9 @@ int batch_occupancy()
 cudaError_t launch_batch(const FusedArgs* d_reqs, const BatchTile* d_tiles, const uint32_t* d_ntiles,
                          uint32_t* d_counter, int grid, cudaStream_t st)
 {
-    static bool attr_set = false;  // setting the attribute twice is harmless
     const size_t sm = batch_smem_ct();
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(stft_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    const cudaError_t e = ensure_smem_attr<stft_batch_kernel>(sm);
+    if (e != cudaSuccess) return e;
     stft_batch_kernel<<<grid, 256, sm, st>>>(d_reqs, d_tiles, d_ntiles, d_counter);
     return cudaGetLastError();
 }

@@ -654,12 +654,8 @@ cudaError_t launch_fused_t(const FusedArgs& a, int grid, cudaStream_t st)
         if constexpr (fused_staged(EXP) && OUTK != OUT_PLANES) {
             constexpr size_t sm = staged_smem_bytes_ct(EXP, OUTK);
             auto k = stft_staged_kernel<EXP, OUTK>;
-            static bool attr_set = false;  // setting the attribute twice is harmless
-            if (!attr_set) {
-                cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-                if (e != cudaSuccess) return e;
-                attr_set = true;
-            }
+            const cudaError_t e = ensure_smem_attr<stft_staged_kernel<EXP, OUTK>>(sm);
+            if (e != cudaSuccess) return e;
             k<<<grid, threads, sm, st>>>(a);
             return cudaGetLastError();
         } else {
@@ -668,12 +664,8 @@ cudaError_t launch_fused_t(const FusedArgs& a, int grid, cudaStream_t st)
     } else {
         constexpr size_t sm = fused_smem_bytes_ct(EXP);
         auto k = stft_fused_kernel<EXP, OUTK>;
-        static bool attr_set = false;
-        if (!attr_set) {
-            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-            if (e != cudaSuccess) return e;
-            attr_set = true;
-        }
+        const cudaError_t e = ensure_smem_attr<stft_fused_kernel<EXP, OUTK>>(sm);
+        if (e != cudaSuccess) return e;
         k<<<grid, threads, sm, st>>>(a);
         return cudaGetLastError();
     }

@@ -292,12 +292,8 @@ cudaError_t launch_columns_t(const LargeArgs& a, uint64_t frames, cudaStream_t s
     constexpr int T = fused_M(EXP1) / fused_cfg(EXP1).R;
     constexpr size_t smem = (size_t)kTileC * large_col_stride(EXP1) * sizeof(float2);
     auto k = large_columns_kernel<EXP1>;
-    static bool attr = false;
-    if (!attr) {
-        const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    const cudaError_t e = ensure_smem_attr<large_columns_kernel<EXP1>>(smem);
+    if (e != cudaSuccess) return e;
     constexpr int FPC = large_col_frames(EXP1);
     const uint64_t grid = (frames + FPC - 1) / FPC * (a.m2 / kTileC);
     LargeArgs b = a;
@@ -312,12 +308,8 @@ cudaError_t launch_rows_t(const LargeArgs& a, uint64_t frames, cudaStream_t st)
     constexpr int T = fused_M(EXP2) / fused_cfg(EXP2).R;
     constexpr size_t smem = (size_t)2 * kTileR * large_row_stride(EXP2) * sizeof(float2);
     auto k = large_rows_kernel<EXP2, OUTK>;
-    static bool attr = false;
-    if (!attr) {
-        const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    const cudaError_t e = ensure_smem_attr<large_rows_kernel<EXP2, OUTK>>(smem);
+    if (e != cudaSuccess) return e;
     const uint64_t grid = frames * (a.m1 / (2 * kTileR));
     k<<<(unsigned)grid, 2 * kTileR * T, smem, st>>>(a);
     return cudaGetLastError();

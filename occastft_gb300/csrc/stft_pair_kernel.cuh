@@ -377,12 +377,8 @@ cudaError_t launch_pair_t(const FusedArgs& a, int grid, cudaStream_t st)
         constexpr int threads = pair_cta_threads(EXP);
         constexpr size_t sm = pair_smem_bytes_ct(EXP);
         auto k = stft_pair_kernel<EXP, OUTK>;
-        static bool attr_set = false;  // setting the attribute twice is harmless
-        if (!attr_set) {
-            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-            if (e != cudaSuccess) return e;
-            attr_set = true;
-        }
+        const cudaError_t e = ensure_smem_attr<stft_pair_kernel<EXP, OUTK>>(sm);
+        if (e != cudaSuccess) return e;
         k<<<grid, threads, sm, st>>>(a);
         return cudaGetLastError();
     } else {

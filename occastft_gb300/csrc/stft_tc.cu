@@ -1395,17 +1395,14 @@ cudaError_t launch_tcg_t(const FusedArgs& a, int* err, int sms, cudaStream_t st)
         return cudaErrorInvalidValue;
     } else {
         auto k = stft_tcg_kernel<P, Q, OUTK, PM>;
-        static int per_sm = 0;
-        if (!per_sm) {
-            cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM);
-            if (e != cudaSuccess) return e;
-            int occ = 0;
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 128, C::SMEM);
-            if (e != cudaSuccess) return e;
-            // CTAs resident on one SM must also fit its 512 tensor-memory columns
-            const int by_tmem = 512 / (int)C::TMEM_COLS;
-            per_sm = occ < 1 ? 1 : (occ < by_tmem ? occ : by_tmem);
-        }
+        cudaError_t e = ensure_smem_attr<stft_tcg_kernel<P, Q, OUTK, PM>>(C::SMEM);
+        if (e != cudaSuccess) return e;
+        int occ = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, 128, C::SMEM);
+        if (e != cudaSuccess) return e;
+        // CTAs resident on one SM must also fit its 512 tensor-memory columns
+        const int by_tmem = 512 / (int)C::TMEM_COLS;
+        const int per_sm = occ < 1 ? 1 : (occ < by_tmem ? occ : by_tmem);
         const uint64_t ntiles = (a.frames + C::FPT - 1) / C::FPT;
         const uint64_t cap = (uint64_t)sms * per_sm;
         const uint64_t grid = ntiles < cap ? ntiles : cap;
@@ -1433,16 +1430,21 @@ cudaError_t launch_tcg_p(int pm, int outk, const FusedArgs& a, int* err, int sms
 template <int R, int PM>
 const unsigned char* tc_tables(cudaError_t* e)
 {
-    // built once per process (one device per runner context); a failed build
-    // (say, attempted while another stream was capturing a graph) is retried
-    // by the next call instead of being remembered
+    // built once per device (the image is a __device__ array, one per
+    // device); a failed build (say, attempted while another stream was
+    // capturing a graph) is retried by the next call instead of being remembered
     static std::mutex mu;
-    static bool built = false;
-    static unsigned char* img = nullptr;
+    static unsigned char* img[64] = {};
+    int dev = 0;
+    cudaError_t rd = cudaGetDevice(&dev);
+    if (rd != cudaSuccess || dev < 0 || dev >= 64) {
+        *e = rd != cudaSuccess ? rd : cudaErrorInvalidDevice;
+        return nullptr;
+    }
     std::lock_guard<std::mutex> lk(mu);
-    if (built) {
+    if (img[dev]) {
         *e = cudaSuccess;
-        return img;
+        return img[dev];
     }
     void* p = nullptr;
     cudaError_t r;
@@ -1465,9 +1467,8 @@ const unsigned char* tc_tables(cudaError_t* e)
     }
     *e = r;
     if (r != cudaSuccess) return nullptr;
-    img = static_cast<unsigned char*>(p);
-    built = true;
-    return img;
+    img[dev] = static_cast<unsigned char*>(p);
+    return img[dev];
 }
 
 template <int R, int OUTK, int PM>
@@ -1478,12 +1479,8 @@ cudaError_t launch_tc2_t(const FusedArgs& a, int* err, int test_stall, int sms, 
     const unsigned char* tab = tc_tables<R, PM>(&e);
     if (e != cudaSuccess) return e;
     auto k = stft_tc2_kernel<R, OUTK, PM>;
-    static bool attr = false;
-    if (!attr) {
-        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    e = ensure_smem_attr<stft_tc2_kernel<R, OUTK, PM>>(C::SMEM);
+    if (e != cudaSuccess) return e;
     // one CTA per SM: its tensor memory (TMEM_COLS) and shared memory
     const uint64_t ntiles = (a.frames + C::FPT - 1) / C::FPT;
     const uint64_t grid = ntiles < (uint64_t)sms ? ntiles : (uint64_t)sms;
@@ -1512,12 +1509,8 @@ cudaError_t launch_tc_t(const FusedArgs& a, int* err, int sms, cudaStream_t st)
 {
     using C = TcCfg<R>;
     auto k = stft_tc_kernel<R, OUTK>;
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    const cudaError_t e = ensure_smem_attr<stft_tc_kernel<R, OUTK>>(C::SMEM);
+    if (e != cudaSuccess) return e;
     const uint64_t ntiles = (a.frames + C::FPT - 1) / C::FPT;
     // at most two CTAs per SM hold tensor memory at a time (2 x TMEM_COLS <= 512)
     const uint64_t grid = ntiles < (uint64_t)sms * 2 ? ntiles : (uint64_t)sms * 2;

@@ -273,13 +273,8 @@ template <int EXP, int OUTK>
 cudaError_t launch_tpf_t(const FusedArgs& a, int grid, cudaStream_t st)
 {
     auto k = stft_tpf_kernel<EXP, OUTK>;
-    static bool attr_set = false;
-    if (!attr_set) {
-        const cudaError_t e =
-            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TpfCfg<EXP>::SMEM);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    const cudaError_t e = ensure_smem_attr<stft_tpf_kernel<EXP, OUTK>>(TpfCfg<EXP>::SMEM);
+    if (e != cudaSuccess) return e;
     k<<<grid, kTpfThreads, TpfCfg<EXP>::SMEM, st>>>(a);
     return cudaGetLastError();
 }
@@ -571,13 +566,8 @@ template <int EXP, int OUTK>
 cudaError_t launch_tpfl_t(const FusedArgs& a, int grid, cudaStream_t st)
 {
     auto k = stft_tpfl_kernel<EXP, OUTK>;
-    static bool attr_set = false;
-    if (!attr_set) {
-        const cudaError_t e =
-            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TplCfg<EXP>::SMEM);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    const cudaError_t e = ensure_smem_attr<stft_tpfl_kernel<EXP, OUTK>>(TplCfg<EXP>::SMEM);
+    if (e != cudaSuccess) return e;
     k<<<grid, TplCfg<EXP>::THREADS, TplCfg<EXP>::SMEM, st>>>(a);
     return cudaGetLastError();
 }
