@@ -637,9 +637,20 @@ int batch_build(ocs_request* reqs, int count, BatchPlan& bp, bool write_status)
         const Request& r = bp.parsed[i];
         return r.opt.half_complex ? ocs::OUT_HALF : (r.opt.serial_power ? ocs::OUT_POWER_SERIAL : ocs::OUT_POWER);
     };
+    // tiles ordered by (window size, output kind, window table): a CTA's
+    // successive tiles then mostly share one code path and one window table,
+    // which the batch kernel keeps in shared memory between tiles
+    auto win_key = [&](int i) {
+        const Request& r = bp.parsed[i];
+        uint32_t sb;
+        std::memcpy(&sb, &r.opt.sigma, sizeof sb);
+        return std::make_tuple(r.opt.window, sb);
+    };
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
         const int ea = bp.parsed[a].exp, eb = bp.parsed[b].exp;
-        return ea != eb ? ea < eb : outk_of(a) < outk_of(b);
+        if (ea != eb) return ea < eb;
+        if (outk_of(a) != outk_of(b)) return outk_of(a) < outk_of(b);
+        return win_key(a) < win_key(b);
     });
     for (int i : order) {
         const Request& r = bp.parsed[i];

@@ -63,11 +63,15 @@ __device__ __forceinline__ void batch_tile(const FusedArgs& a, uint64_t f0, uint
         constexpr int TWN = fused_tw_size(EXP);
         float2* st = reinterpret_cast<float2*>(reinterpret_cast<char*>(smem) + batch_frames_smem());
         float2* sw = st + TWN;
-        // every thread sees the same pointers: a uniform branch
-        if (*s_tw != a.tw || *s_win != a.win) {
+        // every thread sees the same pointers: uniform branches; only the
+        // table that differs from the previous tile's is copied
+        const bool new_tw = *s_tw != a.tw, new_win = *s_win != a.win;
+        if (new_tw || new_win) {
             __syncthreads();  // the previous tile's table reads are over
-            for (int i = tid; i < TWN; i += 256) st[i] = a.tw[i];
-            for (int i = tid; i < (1 << EXP) / 2; i += 256) sw[i] = win2[i];
+            if (new_tw)
+                for (int i = tid; i < TWN; i += 256) st[i] = a.tw[i];
+            if (new_win)
+                for (int i = tid; i < (1 << EXP) / 2; i += 256) sw[i] = win2[i];
             __syncthreads();
             if (tid == 0) {
                 *s_tw = a.tw;

@@ -336,13 +336,19 @@ stft_pair_kernel(const FusedArgs a)
                 const float pb = power_of<OUTK>(B);
                 if (!a.dense) {
                     float* ra = a.out + fa * (uint64_t)N;
-                    if (act_a) {
+                    // slots 0 < u < R/2 hold T <= k < H: both mirror bins exist
+                    constexpr bool inner = u != 0 && u != R / 2;
+                    const bool mirror = inner || (k != 0 && k != H);
+                    if (act_b) {  // both frames of the pair (act_b implies act_a)
                         __stcs(ra + k, pa);
-                        if (k != 0 && k != H) __stcs(ra + (N - k), pa);
-                    }
-                    if (act_b) {
                         __stcs(ra + N + k, pb);
-                        if (k != 0 && k != H) __stcs(ra + N + (N - k), pb);
+                        if (mirror) {
+                            __stcs(ra + (N - k), pa);
+                            __stcs(ra + N + (N - k), pb);
+                        }
+                    } else if (act_a) {
+                        __stcs(ra + k, pa);
+                        if (mirror) __stcs(ra + (N - k), pa);
                     }
                 } else {
                     float* ra = a.out + fa * (uint64_t)(H + 1);
