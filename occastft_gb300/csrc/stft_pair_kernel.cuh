@@ -19,6 +19,7 @@ namespace ocs {
 
 // ------------------------------------------------------------ plan
 __host__ __device__ constexpr int pair_R(int exp) { return exp <= 6 ? 16 : 32; }
+__host__ __device__ constexpr int pair_min_blocks(int exp);
 
 __host__ __device__ constexpr FusedCfg pair_cfg(int exp)
 {
@@ -54,6 +55,13 @@ __host__ __device__ constexpr int pair_ppc(int exp) { return pair_cta_threads(ex
 __host__ __device__ constexpr int pair_buf_stride(int exp) { return (1 << exp) + (1 << exp) / pair_R(exp) + 1; }
 __host__ __device__ constexpr bool pair_tables_in_smem(int exp) { return exp <= 11; }
 __host__ __device__ constexpr bool pair_supported(int exp) { return exp >= 6 && exp <= 14; }
+// 2 x 256 threads per SM below 2^14 (R = 16 at 2^10, three 256-thread CTAs
+// of up to 80 registers, measured 300 against 390 Gsamples/s: the extra
+// block-wide exchange costs more than the occupancy gains)
+__host__ __device__ constexpr int pair_min_blocks(int exp)
+{
+    return pair_cta_threads(exp) >= 512 ? 1 : 512 / pair_cta_threads(exp);
+}
 // Twiddle entries copied to shared memory: the whole table up to 2^11; above,
 // the first exchange stage's (31 x 32 entries, 7.9 KB), which next to the
 // window still fits beside the exchange buffers at the same occupancy; the
@@ -260,7 +268,7 @@ __device__ __forceinline__ void pair_tables(const FusedArgs& a, float2* s_tab, i
 }
 
 template <int EXP, int OUTK>
-__global__ void __launch_bounds__(pair_cta_threads(EXP), (pair_cta_threads(EXP) >= 512 ? 1 : 512 / pair_cta_threads(EXP)))
+__global__ void __launch_bounds__(pair_cta_threads(EXP), pair_min_blocks(EXP))
 stft_pair_kernel(const FusedArgs a)
 {
     using K = PairCore<EXP>;
