@@ -1197,19 +1197,45 @@ __global__ void __launch_bounds__(128, 1) stft_tcg_kernel(const FusedArgs a, int
             const uint64_t f = f0 + lf;
             const bool act = f < a.frames;
             const uint64_t s0 = f * a.hop;
+            // the lane's 8 windowed samples [8c, 8c+8): two float4 loads of
+            // samples and of window when the frame lies inside the signal and
+            // both start on 16 bytes, else one bounded load each
+            const bool vec = act && s0 + N <= a.n && a.win &&
+                             ((reinterpret_cast<uintptr_t>(a.x + s0) | reinterpret_cast<uintptr_t>(a.win)) & 15) == 0;
+            auto load8 = [&](int c, float (&v)[8]) {
+                if (vec) {
+                    const float4* xp = reinterpret_cast<const float4*>(a.x + s0 + 8 * c);
+                    const float4* wp = reinterpret_cast<const float4*>(a.win + 8 * c);
+                    const float4 x0 = xp[0], x1 = xp[1], w0 = wp[0], w1 = wp[1];
+                    v[0] = x0.x * w0.x;
+                    v[1] = x0.y * w0.y;
+                    v[2] = x0.z * w0.z;
+                    v[3] = x0.w * w0.w;
+                    v[4] = x1.x * w1.x;
+                    v[5] = x1.y * w1.y;
+                    v[6] = x1.z * w1.z;
+                    v[7] = x1.w * w1.w;
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const int i = 8 * c + q;
+                        const uint64_t gi = s0 + i;
+                        float t = (act && gi < a.n) ? a.x[gi] : 0.0f;
+                        if (a.win) t *= a.win[i];
+                        v[q] = t;
+                    }
+                }
+            };
             // first read: sum, minimum and maximum of the windowed frame
             float sum = 0.0f, mn = 0.0f, mx = 0.0f;
             for (int j = 0; j < N / 256; ++j) {  // lane owns samples [8c, 8c+8), c = lane + 32 j
-                const int c = lane + 32 * j;
+                float v[8];
+                load8(lane + 32 * j, v);
 #pragma unroll
                 for (int q = 0; q < 8; ++q) {
-                    const int i = 8 * c + q;
-                    const uint64_t gi = s0 + i;
-                    float v = (act && gi < a.n) ? a.x[gi] : 0.0f;
-                    if (a.win) v *= a.win[i];
-                    sum += v;
-                    mn = fminf(mn, v);
-                    mx = fmaxf(mx, v);
+                    sum += v[q];
+                    mn = fminf(mn, v[q]);
+                    mx = fmaxf(mx, v[q]);
                 }
             }
 #pragma unroll
@@ -1228,14 +1254,9 @@ __global__ void __launch_bounds__(128, 1) stft_tcg_kernel(const FusedArgs a, int
             for (int j = 0; j < N / 256; ++j) {
                 const int c = lane + 32 * j;
                 float v[8];
+                load8(c, v);
 #pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    const int i = 8 * c + q;
-                    const uint64_t gi = s0 + i;
-                    float x = (act && gi < a.n) ? a.x[gi] : 0.0f;
-                    if (a.win) x *= a.win[i];
-                    v[q] = (x - mean) * sc;
-                }
+                for (int q = 0; q < 8; ++q) v[q] = (v[q] - mean) * sc;
                 uint4 pp[PARTS];
                 S::split8(v, pp);
                 // samples 8c .. 8c+7 = (g0 .. g0+7, m) with g = i mod Q, m = i / Q
