@@ -1,4 +1,4 @@
-// Thread-per-frame STFT for window 2^6 (sm_103a).
+// Thread-per-frame STFT for windows 2^6 .. 2^8 (sm_103a).
 //
 // At N = 64 the cooperative kernels spend most of their instructions on
 // moving data between the threads that share a frame (shuffles, exchange
@@ -8,14 +8,14 @@
 //   * a warp takes 32 consecutive frames; their samples arrive by cp.async in
 //     32 shared-memory rows of N + 4 floats (16-byte chunks, zero-filled past
 //     the signal end or the last frame);
-//   * lane i reads row i with 16-byte loads (the +4 padding makes the eight
-//     lanes of each quarter-warp hit disjoint banks), applies the window
+//   * lane i reads row i with 16-byte loads (the +4 padding puts the rows
+//     that a quarter-warp reads at one column on distinct banks), applies the window
 //     (pre-scaled by 1/2, as in the fused kernels), removes the mean, runs a
 //     32-point DFT in registers and untangles with compile-time twiddles;
 //   * the N output floats go back into the same row with 16-byte stores and
 //     leave as one coalesced block of 32 frames.
 // Outputs: power (|X| or the Serial runner's sqrt(2)|Re X|) in the reference
-// layout or the dense layout.  Half-complex stays with the cooperative kernels.
+// layout or the dense layout; at N = 64 also half-complex (tpf_half_out).
 //
 // Windows 2^7 and 2^8 use L = N / 64 lanes per frame (stft_tpfl_kernel): the
 // packed M-point complex FFT (M = N / 2 = 32 L) starts with one radix-L
@@ -26,9 +26,9 @@
 // Z[k] with Z[M - k]; for L = 2 both sit in the same lane, for L = 4 lanes 1
 // and 3 swap their upper 16 slots with one shuffle each.  Each lane then owns
 // the bins congruent to +-q mod L and writes them into the frame's row.
-// It is the same pipeline as the fused kernels (Overlap_Common, Window_*,
-// DCRemove_Common, Stockham FFT, toPower; OKL/EXPCommon.okl:7-245,
-// OKL/kernel.okl:178-194).
+// Windows 2^7 and 2^8 produce power outputs.  It is the same pipeline as the
+// fused kernels (Overlap_Common, Window_*, DCRemove_Common, Stockham FFT,
+// toPower / toHalfComplexFormat; OKL/EXPCommon.okl:7-245, OKL/kernel.okl:178-218).
 #include "stft_fused_kernel.cuh"
 
 namespace ocs {
