@@ -82,7 +82,8 @@ size_t batch_smem_bytes();
 cudaError_t launch_batch(const FusedArgs* d_reqs, const BatchTile* d_tiles, const uint32_t* d_ntiles,
                          uint32_t* d_counter, int grid, cudaStream_t st);
 
-// thread-per-frame kernel (window 2^6, power outputs)
+// lanes-per-frame kernels: N/64 lanes per frame, the FFT in registers
+// (power at windows 2^6 .. 2^8, half-complex at 2^6)
 bool tpf_has(int exp, int outk);
 int tpf_frames_per_cta(int exp);
 int tpf_occupancy(int exp, int outk);
