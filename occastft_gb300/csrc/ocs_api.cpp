@@ -66,6 +66,7 @@ struct Context {
     cudaStream_t s_setup = nullptr;
     std::map<int, float2*> twiddles;                             // exp * 2 + paired -> table
     std::map<std::tuple<int, int, uint32_t>, float*> windows;    // (kind, exp, sigma bits) -> table
+    std::map<const float*, std::vector<float>> windows_host;     // device table -> host copy (windows <= 2^8)
     std::map<uint64_t, float2*> two_level;                       // L -> exp(-2 pi i j / L) lo|hi table
     std::map<std::pair<int, int>, int> occupancy;                // (exp, output kind) -> CTAs per SM
     std::vector<Slot*> free_slots;
@@ -180,8 +181,18 @@ int get_window(int kind, int exp, float sigma, bool scaled, const float** out)
     OCS_CUDA(cudaMemcpyAsync(d, w.data(), sizeof(float) * w.size(), cudaMemcpyHostToDevice, c.s_setup));
     OCS_CUDA(cudaStreamSynchronize(c.s_setup));
     c.windows[key] = d;
+    if (exp <= 8) c.windows_host[d] = w;  // the lanes-per-frame kernels take it as a parameter
     *out = d;
     return OCS_OK;
+}
+
+// Host copy of a window table that get_window made (windows up to 2^8), or null.
+const float* host_window(const float* d)
+{
+    Context& c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    auto it = c.windows_host.find(d);
+    return it == c.windows_host.end() ? nullptr : it->second.data();
 }
 
 // ---------------------------------------------------------------- kernel choice
@@ -312,7 +323,11 @@ cudaError_t launch_variant(int v, const Request& r, int outk, ocs::FusedArgs a, 
         a.tw = tw_pair;
         return ocs::launch_pair(r.exp, outk, a, grid_size(r.exp, outk, VAR_PAIR, a.frames), st);
     }
-    if (v == VAR_TPF) return ocs::launch_tpf(r.exp, outk, a, grid_size(r.exp, outk, VAR_TPF, a.frames), st);
+    if (v == VAR_TPF) {
+        const float* hw = host_window(a.win);
+        if (!hw) return cudaErrorInvalidValue;
+        return ocs::launch_tpf(r.exp, outk, a, hw, grid_size(r.exp, outk, VAR_TPF, a.frames), st);
+    }
     a.tw = tw_single;
     return ocs::launch_fused(r.exp, outk, v == VAR_STAGED, a, grid_size(r.exp, outk, v, a.frames), st);
 }
@@ -848,6 +863,7 @@ void ocs_shutdown(void)
     for (auto& kv : c.two_level) cudaFree(kv.second);
     c.twiddles.clear();
     c.windows.clear();
+    c.windows_host.clear();
     c.two_level.clear();
     for (Slot* s : c.all_slots) {
         cudaStreamDestroy(s->s_h2d);

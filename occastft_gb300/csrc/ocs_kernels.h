@@ -87,7 +87,9 @@ cudaError_t launch_batch(const FusedArgs* d_reqs, const BatchTile* d_tiles, cons
 bool tpf_has(int exp, int outk);
 int tpf_frames_per_cta(int exp);
 int tpf_occupancy(int exp, int outk);
-cudaError_t launch_tpf(int exp, int outk, const FusedArgs& a, int grid, cudaStream_t st);
+// host_win: the N window coefficients a.win holds (scaled by 1/2), passed to
+// the kernel as a parameter
+cudaError_t launch_tpf(int exp, int outk, const FusedArgs& a, const float* host_win, int grid, cudaStream_t st);
 
 // windows 2^16 .. 2^22: four-step FFT in two launches (column pass, row pass)
 constexpr int kLargeMinExp = 16;

@@ -31,17 +31,28 @@
 // toPower / toHalfComplexFormat; OKL/EXPCommon.okl:7-245, OKL/kernel.okl:178-218).
 #include "stft_fused_kernel.cuh"
 
+#include <cstring>
+
 namespace ocs {
 namespace {
 
 constexpr int kTpfThreads = 256;  // 8 warps, 32 frames each per step
+
+// The window coefficients (scaled by 1/2) as a kernel parameter: every lane
+// reads the same coefficient at a compile-time offset, which the constant
+// cache serves without using the shared-memory / L1 pipe (the kernels are
+// bound by that pipe).  N <= 256: at most 1 KB.
+template <int N>
+struct WinParam {
+    float4 v[N / 4];
+};
 
 template <int EXP>
 struct TpfCfg {
     static constexpr int N = 1 << EXP;
     static constexpr int M = N / 2;
     static constexpr int RS = N + 4;  // row stride in floats (16-byte aligned, conflict-free 16-byte access)
-    static constexpr size_t SMEM = (size_t)N * 4 + (size_t)(kTpfThreads / 32) * 32 * RS * 4;
+    static constexpr size_t SMEM = (size_t)(kTpfThreads / 32) * 32 * RS * 4;
 };
 
 // Half-complex output of the lane's frame (Z[k] in v[k], k < M): the N
@@ -109,17 +120,14 @@ __device__ __forceinline__ void tpf_half_out(const FusedArgs& a, const float2 (&
 }
 
 template <int EXP, int OUTK>
-__global__ void __launch_bounds__(kTpfThreads, 2) stft_tpf_kernel(const FusedArgs a)
+__global__ void __launch_bounds__(kTpfThreads, 2) stft_tpf_kernel(const FusedArgs a, const WinParam<1 << EXP> wp)
 {
     using C = TpfCfg<EXP>;
     constexpr int N = C::N, M = C::M, RS = C::RS;
     static_assert(OUTK == OUT_POWER || OUTK == OUT_POWER_SERIAL || OUTK == OUT_HALF, "power or half-complex");
     extern __shared__ float4 smem4[];
-    float* s_win = reinterpret_cast<float*>(smem4);  // N floats, window x 1/2
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    float* rows = s_win + N + warp * 32 * RS;
-    for (int i = tid; i < N; i += kTpfThreads) s_win[i] = a.win[i];
-    __syncthreads();
+    float* rows = reinterpret_cast<float*>(smem4) + warp * 32 * RS;
 
     const int cs = a.cs;  // bytes per async copy: 16, 8 or 4
     const int per_chunk = cs / 4;
@@ -185,7 +193,7 @@ __global__ void __launch_bounds__(kTpfThreads, 2) stft_tpf_kernel(const FusedArg
 #pragma unroll
         for (int j = 0; j < M / 2; ++j) {
             const float4 d = *reinterpret_cast<const float4*>(row + 4 * j);
-            const float4 w = *reinterpret_cast<const float4*>(s_win + 4 * j);
+            const float4 w = wp.v[j];
             v[2 * j] = make_float2(d.x * w.x, d.y * w.y);
             v[2 * j + 1] = make_float2(d.z * w.z, d.w * w.w);
         }
@@ -269,13 +277,21 @@ __global__ void __launch_bounds__(kTpfThreads, 2) stft_tpf_kernel(const FusedArg
     cp_async_wait_all();
 }
 
+template <int N>
+WinParam<N> win_param(const float* host_win)
+{
+    WinParam<N> w;
+    std::memcpy(&w, host_win, sizeof w);
+    return w;
+}
+
 template <int EXP, int OUTK>
-cudaError_t launch_tpf_t(const FusedArgs& a, int grid, cudaStream_t st)
+cudaError_t launch_tpf_t(const FusedArgs& a, const float* host_win, int grid, cudaStream_t st)
 {
     auto k = stft_tpf_kernel<EXP, OUTK>;
     const cudaError_t e = ensure_smem_attr<stft_tpf_kernel<EXP, OUTK>>(TpfCfg<EXP>::SMEM);
     if (e != cudaSuccess) return e;
-    k<<<grid, kTpfThreads, TpfCfg<EXP>::SMEM, st>>>(a);
+    k<<<grid, kTpfThreads, TpfCfg<EXP>::SMEM, st>>>(a, win_param<1 << EXP>(host_win));
     return cudaGetLastError();
 }
 
@@ -342,25 +358,24 @@ struct TplCfg {
     static constexpr int RS = N + 4;
     static constexpr int ORS = N + L;     // output row stride (L j + q distinct banks)
     static constexpr int THREADS = 256;   // 8 warps; two CTAs per SM (128 registers)
-    static constexpr size_t SMEM = (size_t)N * 4 + (size_t)(32 + 17) * L * 8 + (size_t)(THREADS / 32) * F * RS * 4;
+    static constexpr size_t SMEM = (size_t)(32 + 17) * L * 8 + (size_t)(THREADS / 32) * F * RS * 4;
     static_assert((F - 1) * ORS + N <= F * RS, "output rows fit in the input rows");
 };
 
 template <int EXP, int OUTK>
-__global__ void __launch_bounds__(TplCfg<EXP>::THREADS, 2) stft_tpfl_kernel(const FusedArgs a)
+__global__ void __launch_bounds__(TplCfg<EXP>::THREADS, 2) stft_tpfl_kernel(const FusedArgs a,
+                                                                             const WinParam<1 << EXP> wp)
 {
     using C = TplCfg<EXP>;
     constexpr int N = C::N, M = C::M, L = C::L, F = C::F, RS = C::RS, ORS = C::ORS, NT = C::THREADS;
     static_assert(OUTK == OUT_POWER || OUTK == OUT_POWER_SERIAL, "power outputs only");
     static_assert(L == 2 || L == 4, "windows 2^7 and 2^8");
     extern __shared__ float4 smem4[];
-    float* s_win = reinterpret_cast<float*>(smem4);  // N floats, window x 1/2
-    float2* s_tw1 = reinterpret_cast<float2*>(s_win + N);
+    float2* s_tw1 = reinterpret_cast<float2*>(smem4);
     float2* s_tw2 = s_tw1 + 32 * L;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int q = lane % L, jf = lane / L;  // lane q of the warp's frame jf
     float* const rows = reinterpret_cast<float*>(s_tw2 + 17 * L) + warp * F * RS;
-    for (int i = tid; i < N; i += NT) s_win[i] = a.win[i];
     const TplTab<EXP>& tab = tpl_tab<EXP>();
     for (int i = tid; i < 32 * L; i += NT) s_tw1[i] = make_float2(tab.tw1[2 * i], tab.tw1[2 * i + 1]);
     for (int i = tid; i < 17 * L; i += NT) s_tw2[i] = make_float2(tab.tw2[2 * i], tab.tw2[2 * i + 1]);
@@ -445,7 +460,7 @@ __global__ void __launch_bounds__(TplCfg<EXP>::THREADS, 2) stft_tpfl_kernel(cons
 #pragma unroll
             for (int p = 0; p < L; ++p) {
                 const float4 d = *reinterpret_cast<const float4*>(row + 64 * p + 4 * c);
-                const float4 w = *reinterpret_cast<const float4*>(s_win + 64 * p + 4 * c);
+                const float4 w = wp.v[16 * p + c];
                 y0[p] = make_float2(d.x * w.x, d.y * w.y);
                 y1[p] = make_float2(d.z * w.z, d.w * w.w);
             }
@@ -563,12 +578,12 @@ __global__ void __launch_bounds__(TplCfg<EXP>::THREADS, 2) stft_tpfl_kernel(cons
 }
 
 template <int EXP, int OUTK>
-cudaError_t launch_tpfl_t(const FusedArgs& a, int grid, cudaStream_t st)
+cudaError_t launch_tpfl_t(const FusedArgs& a, const float* host_win, int grid, cudaStream_t st)
 {
     auto k = stft_tpfl_kernel<EXP, OUTK>;
     const cudaError_t e = ensure_smem_attr<stft_tpfl_kernel<EXP, OUTK>>(TplCfg<EXP>::SMEM);
     if (e != cudaSuccess) return e;
-    k<<<grid, TplCfg<EXP>::THREADS, TplCfg<EXP>::SMEM, st>>>(a);
+    k<<<grid, TplCfg<EXP>::THREADS, TplCfg<EXP>::SMEM, st>>>(a, win_param<1 << EXP>(host_win));
     return cudaGetLastError();
 }
 
@@ -598,15 +613,19 @@ int tpf_frames_per_cta(int exp)
     return kTpfThreads;
 }
 
-cudaError_t launch_tpf(int exp, int outk, const FusedArgs& a, int grid, cudaStream_t st)
+cudaError_t launch_tpf(int exp, int outk, const FusedArgs& a, const float* host_win, int grid, cudaStream_t st)
 {
-    if (outk == OUT_HALF) return exp == 6 ? launch_tpf_t<6, OUT_HALF>(a, grid, st) : cudaErrorInvalidValue;
+    if (!host_win) return cudaErrorInvalidValue;
+    const float* hw = host_win;
+    if (outk == OUT_HALF) return exp == 6 ? launch_tpf_t<6, OUT_HALF>(a, hw, grid, st) : cudaErrorInvalidValue;
     const bool ser = outk == OUT_POWER_SERIAL;
     if (outk != OUT_POWER && !ser) return cudaErrorInvalidValue;
     switch (exp) {
-    case 6: return ser ? launch_tpf_t<6, OUT_POWER_SERIAL>(a, grid, st) : launch_tpf_t<6, OUT_POWER>(a, grid, st);
-    case 7: return ser ? launch_tpfl_t<7, OUT_POWER_SERIAL>(a, grid, st) : launch_tpfl_t<7, OUT_POWER>(a, grid, st);
-    case 8: return ser ? launch_tpfl_t<8, OUT_POWER_SERIAL>(a, grid, st) : launch_tpfl_t<8, OUT_POWER>(a, grid, st);
+    case 6: return ser ? launch_tpf_t<6, OUT_POWER_SERIAL>(a, hw, grid, st) : launch_tpf_t<6, OUT_POWER>(a, hw, grid, st);
+    case 7:
+        return ser ? launch_tpfl_t<7, OUT_POWER_SERIAL>(a, hw, grid, st) : launch_tpfl_t<7, OUT_POWER>(a, hw, grid, st);
+    case 8:
+        return ser ? launch_tpfl_t<8, OUT_POWER_SERIAL>(a, hw, grid, st) : launch_tpfl_t<8, OUT_POWER>(a, hw, grid, st);
     default: return cudaErrorInvalidValue;
     }
 }
