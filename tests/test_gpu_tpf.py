@@ -25,7 +25,8 @@ def test_tpf_sizes_and_advances(tpf, ocs_lib, orc, exp, n, ov):
     for opts in ("--hamming_window", "--hanning_window --remove_dc", "--blackman_window --layout=dense",
                  "--flattop_window --serial_power", "--nuttall_window --remove_dc --layout=dense",
                  "--hamming_window --half_complex_return",
-                 "--blackman_window --remove_dc --half_complex_return --layout=dense"):
+                 "--blackman_window --remove_dc --half_complex_return --layout=dense",
+                 "--gaussian_window=x0.4<<sigma --remove_dc"):
         got = ocs_lib.activate(x, exp, ov, opts)
         ref = orc.fp64_stft(x, exp, ov, opts)
         assert got.size == ref.size
@@ -51,3 +52,37 @@ def test_tpf_matches_other_kernels(tpf, ocs_lib, monkeypatch, exp):
     monkeypatch.setenv("OCS_KERNEL", "single")
     ref = ocs_lib.activate(x, exp, 0.5, "--hanning_window --remove_dc")
     np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-6 * float(np.abs(ref).max()))
+
+
+REINIT_CHILD = r'''
+import sys
+import numpy as np
+sys.path.insert(0, {root!r})
+import occastft_gb300 as ocs
+from oracle import orc
+x = np.random.default_rng(11).uniform(-1, 1, 300_001).astype(np.float32)
+first = [ocs.activate(x, e, 0.5, "--hamming_window") for e in (6, 7, 8)]
+ocs.Runner(0).UnInit()  # frees the plans and window tables
+again = [ocs.activate(x, e, 0.5, "--hamming_window") for e in (6, 7, 8)]
+same = all(np.array_equal(a, b) for a, b in zip(first, again))
+err = max(orc.rel_l2(g, orc.fp64_stft(x, e, 0.5, "--hamming_window")) for g, e in zip(again, (6, 7, 8)))
+print("SAME", same, "ERR", err)
+'''
+
+
+def test_tpf_after_reinit():
+    """The lanes-per-frame kernels take the window from a host copy kept beside
+    the device table; after a shutdown and re-initialisation (new device
+    tables) they still get the right coefficients."""
+    import os
+    import subprocess
+    import sys
+    from tests.conftest import ROOT
+    e = dict(os.environ, OCS_KERNEL="tpf", OCS_AUTOTUNE="0")
+    out = subprocess.run([sys.executable, "-c", REINIT_CHILD.format(root=ROOT)], env=e, capture_output=True,
+                         text=True, timeout=300)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = out.stdout.strip().splitlines()[-1].split()
+    assert line[1] == "True", line
+    assert float(line[3]) <= REL_L2, line
+
