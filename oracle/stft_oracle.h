@@ -12,7 +12,7 @@
  *       bit-for-bit against the reference's own code compiled from source
  *       (oracle/build_ref.sh) and against the committed golden vectors.
  *   orc_fp64_stft — the same framing and window coefficients, with DC removal
- *       and the FFT done in double precision: the accuracy judge.
+ *       and the FFT done in double precision: the accuracy reference.
  */
 #ifndef OCS_STFT_ORACLE_H
 #define OCS_STFT_ORACLE_H
