@@ -335,7 +335,7 @@ def run_batch_leg(ocs, steps: int, warmup: int, count: int = 4096):
            "algorithmic_bytes": int(alg), "launches_per_batch": 1,
            "plain_per_request_gsamples_s": round(total / dt_plain / 1e9, 2),
            "speedup_vs_per_request": round(dt_plain / dt, 2),
-           "workload": "4096 signals, lengths log-uniform [2^12, 2^22], windows {256..4096}, overlap "
+           "workload": f"{count} signals, lengths log-uniform [2^12, 2^22], windows {{256..4096}}, overlap "
                        "{0.25,0.5,0.75}, Hann/Hamming/Blackman, noise + 100 Hz->10 kHz chirp; power, reference "
                        "layout; one CUDA-graph-captured persistent launch vs one fused launch per request"}
     del out, sig
@@ -793,7 +793,7 @@ def run_ours(args):
         tc = run_tc_leg(ocs, x, n, d_out, stream)
     batch = None
     if rank == 0 and not args.no_batch:
-        batch = run_batch_leg(ocs, steps=5, warmup=3)
+        batch = run_batch_leg(ocs, steps=5, warmup=3, count=args.batch_count)
     serving = None
     if rank == 0 and not args.no_serve:
         serving = run_serving_leg(ocs)
@@ -859,6 +859,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-count", type=int, default=4096, help="requests in the uneven batch (profiling runs use fewer)")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--n", type=int, default=N_SAMPLES, help="signal samples (profiling runs use fewer)")
     ap.add_argument("--exp", type=int, default=HEAD_EXP)
