@@ -681,6 +681,7 @@ int batch_build(ocs_request* reqs, int count, BatchPlan& bp, bool write_status)
         a.frames = r.geo.frames;
         a.win = win;
         a.tw = tw;
+        if (ocs::pair_has(r.exp)) get_twiddles(r.exp, true, &a.tw_pair);
         a.out = q.out;
         a.ohalf = r.opt.half_complex && !r.opt.dense ? r.geo.ohalf : 0;
         a.dense = r.opt.dense;

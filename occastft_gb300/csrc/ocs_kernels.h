@@ -41,6 +41,7 @@ struct FusedArgs {
     uint64_t frames;       // frames to compute
     const float* win;      // window table scaled by 1/2 (N floats), never null
     const float2* tw;      // twiddle table of the plan
+    const float2* tw_pair; // batch kernel: the two-frames-per-FFT plan's table (null: not used)
     float* out;            // output (or real plane)
     float* out_im;         // imaginary plane (planes mode)
     uint64_t ohalf;        // compat half-complex: number of complex outputs

@@ -7,7 +7,7 @@
 // output kind is read per request.  Tiles are ordered by (window, output
 // kind) on the host so that concurrently running CTAs mostly share one code
 // path.
-#include "stft_fused_kernel.cuh"
+#include "stft_pair_kernel.cuh"
 
 namespace ocs {
 
@@ -18,10 +18,19 @@ __host__ __device__ constexpr size_t batch_group_smem(int exp)
 {
     return (size_t)fused_fpc(exp) * fused_buf_stride(exp) * 8 + (size_t)(256 / 32) * 4 + 16;
 }
+// power tiles of windows 2^9 and 2^10 run the two-frames-per-FFT body
+__host__ __device__ constexpr bool batch_pair_exp(int exp) { return exp == 9 || exp == 10; }
+__host__ __device__ constexpr size_t batch_pair_smem(int exp)
+{
+    return (size_t)pair_ppc(exp) * pair_buf_stride(exp) * 8 + (size_t)(256 / 32) * 8 + 16;
+}
 __host__ __device__ constexpr size_t batch_frames_smem()
 {
     size_t m = 0;
-    for (int e = kBatchMinExp; e <= kBatchMaxExp; ++e) m = batch_group_smem(e) > m ? batch_group_smem(e) : m;
+    for (int e = kBatchMinExp; e <= kBatchMaxExp; ++e) {
+        m = batch_group_smem(e) > m ? batch_group_smem(e) : m;
+        if (batch_pair_exp(e)) m = batch_pair_smem(e) > m ? batch_pair_smem(e) : m;
+    }
     return (m + 15) / 16 * 16;
 }
 // Twiddle and window tables of windows up to 2^11 are copied into shared
@@ -38,6 +47,7 @@ __host__ __device__ constexpr size_t batch_tab_smem()
     for (int e = kBatchMinExp; e <= kBatchSmemTabMaxExp; ++e) {
         const size_t b = (size_t)fused_tw_size(e) * 8 + ((size_t)1 << e) * 4;
         m = b > m ? b : m;
+        if (batch_pair_exp(e)) m = pair_tab_bytes(e) > m ? pair_tab_bytes(e) : m;
     }
     return m;
 }
@@ -48,6 +58,39 @@ __device__ __forceinline__ void batch_tile(const FusedArgs& a, uint64_t f0, uint
                                            const float2** s_tw, const float** s_win)
 {
     static_assert(fused_cta_threads(EXP) == 256, "batch CTAs have 256 threads");
+    if constexpr (batch_pair_exp(EXP)) {
+        if (a.outk == OUT_POWER && a.tw_pair) {
+            // two frames per FFT: pairs f0/2 .. of the tile (f0 and nf are even
+            // multiples of the CTA's pairs), the pair plan's tables and the
+            // window resident behind the frame buffers
+            static_assert(pair_cta_threads(EXP) == 256, "batch CTAs have 256 threads");
+            constexpr int PPC = pair_ppc(EXP), BS = pair_buf_stride(EXP), T = pair_T(EXP);
+            constexpr int TWN = pair_smem_tw_entries(EXP);
+            const int tid = threadIdx.x;
+            float2* st = reinterpret_cast<float2*>(reinterpret_cast<char*>(smem) + batch_frames_smem());
+            float* sw = reinterpret_cast<float*>(st + TWN);
+            const bool new_tw = *s_tw != a.tw_pair, new_win = *s_win != a.win;
+            if (new_tw || new_win) {
+                __syncthreads();  // the previous tile's table reads are over
+                if (new_tw)
+                    for (int i = tid; i < TWN; i += 256) st[i] = a.tw_pair[i];
+                for (int i = tid; i < (1 << EXP); i += 256) sw[i] = a.win[i];
+                __syncthreads();
+                if (tid == 0) {
+                    *s_tw = a.tw_pair;
+                    *s_win = a.win;
+                }
+            }
+            FusedArgs b = a;
+            b.frames = f0 + nf;  // frames past the tile belong to the next tile
+            b.tw = a.tw_pair;
+            const int lp = tid / T, t = tid - lp * T;
+            const TwTwoLevel tw2{nullptr, nullptr};
+            for (uint64_t pbase = f0 / 2; 2 * pbase < f0 + nf; pbase += PPC)
+                pair_group<EXP, OUT_POWER>(b, pbase, smem + lp * BS, smem + PPC * BS, st, tw2, sw, tid, lp, t);
+            return;
+        }
+    }
     using K = Core<EXP>;
     constexpr int T = K::T;
     constexpr int FPC = fused_fpc(EXP);
@@ -70,7 +113,7 @@ __device__ __forceinline__ void batch_tile(const FusedArgs& a, uint64_t f0, uint
             __syncthreads();  // the previous tile's table reads are over
             if (new_tw)
                 for (int i = tid; i < TWN; i += 256) st[i] = a.tw[i];
-            if (new_win)
+            if (new_win || new_tw)  // the window sits behind the twiddle table
                 for (int i = tid; i < (1 << EXP) / 2; i += 256) sw[i] = win2[i];
             __syncthreads();
             if (tid == 0) {

@@ -268,12 +268,16 @@ __device__ __forceinline__ void pair_tables(const FusedArgs& a, float2* s_tab, i
 }
 
 template <int EXP, int OUTK>
+__device__ __forceinline__ void pair_group(const FusedArgs& a, uint64_t pbase, float2* buf, float2* red,
+                                           const float2* tws, const TwTwoLevel& tw2, const float* win, int tid,
+                                           int lp, int t);
+
+template <int EXP, int OUTK>
 __global__ void __launch_bounds__(pair_cta_threads(EXP), pair_min_blocks(EXP))
 stft_pair_kernel(const FusedArgs a)
 {
     using K = PairCore<EXP>;
-    constexpr int N = K::N, R = K::R, T = K::T;
-    constexpr int H = N / 2;
+    constexpr int T = K::T;
     constexpr int PPC = pair_ppc(EXP);
     constexpr int BS = pair_buf_stride(EXP);
 
@@ -289,7 +293,21 @@ stft_pair_kernel(const FusedArgs a)
     pair_tables<EXP>(a, s_tab, tid, win, tw2);
 
     const uint64_t pairs = (a.frames + 1) / 2;
-    for (uint64_t pbase = (uint64_t)blockIdx.x * PPC; pbase < pairs; pbase += (uint64_t)gridDim.x * PPC) {
+    for (uint64_t pbase = (uint64_t)blockIdx.x * PPC; pbase < pairs; pbase += (uint64_t)gridDim.x * PPC)
+        pair_group<EXP, OUTK>(a, pbase, buf, red, s_tab, tw2, win, tid, lp, t);
+}
+
+// One CTA iteration: pairs pbase .. pbase + PPC - 1 (frames 2p, 2p + 1 below
+// a.frames); buf is this thread's pair buffer, tws the shared-memory twiddles.
+template <int EXP, int OUTK>
+__device__ __forceinline__ void pair_group(const FusedArgs& a, uint64_t pbase, float2* buf, float2* red,
+                                           const float2* tws, const TwTwoLevel& tw2, const float* win, int tid,
+                                           int lp, int t)
+{
+    using K = PairCore<EXP>;
+    constexpr int N = K::N, R = K::R, T = K::T;
+    constexpr int H = N / 2;
+    {
         const uint64_t p = pbase + lp;
         const uint64_t fa = 2 * p, fb = 2 * p + 1;
         const bool act_a = fa < a.frames;
@@ -337,7 +355,7 @@ stft_pair_kernel(const FusedArgs a)
             }
         }
         if (a.remove_dc) K::remove_dc(v, red, tid, lp);
-        K::fft(v, buf, s_tab, a.tw, tw2, t);
+        K::fft(v, buf, tws, a.tw, tw2, t);
         K::partners_prepare(v, buf, t);
         const int src = K::partner_lane(tid, t);
 
