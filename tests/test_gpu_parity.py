@@ -1,7 +1,7 @@
 """Parity of the CUDA path (called through the C ABI) with the oracle and the
 reference's golden vectors.
 
-Bars (the benchmark spec): frame count, offsets, window choice and output layout
+Bars: frame count, offsets, window choice and output layout
 bit-exact; FP32 spectra within REL_L2 = 1e-5 relative L2 of the FP64 oracle
 and of the reference's Serial output (where that output is not the known
 odd-exponent defect)."""
