@@ -129,14 +129,21 @@ typedef struct ocs_request {
 /* Builds the plans (twiddle and window tables) these requests need and grows
  * the batch's descriptor buffers, so that a following ocs_batch_device over
  * requests of the same shapes allocates nothing and can be captured into a
- * CUDA graph.  Replaces nothing in the reference (its runner handles one
- * request at a time, RunnerCommon.cpp:69-134). */
+ * CUDA graph.  It also sets aside descriptor buffers for the next captured
+ * ocs_batch_device: call it once before each capture.  Replaces nothing in
+ * the reference (its runner handles one request at a time,
+ * RunnerCommon.cpp:69-134). */
 int ocs_batch_prepare(const ocs_request* reqs, int count);
 
 /* Runs all valid requests (windows 2^6..2^13) as tiles of one persistent
  * kernel launch on `stream` (requests with larger windows get their own
  * fused launch on the same stream).  Asynchronous.  Returns OCS_OK when the
- * launch was issued; per-request problems land in reqs[i].status. */
+ * launch was issued; per-request problems land in reqs[i].status.
+ * Under stream capture it uses the buffers the last ocs_batch_prepare set
+ * aside (OCS_ENOMEM if there are none, or they are too small) and keeps them
+ * until ocs_shutdown, so the graph replays its own requests whatever batches
+ * run after the capture.  Replays of one graph must not overlap each other on
+ * the GPU (they share those buffers); replays and other batches may. */
 int ocs_batch_device(ocs_request* reqs, int count, void* stream);
 
 /* Same as ocs_batch_device, for callers that must not allocate GPU memory

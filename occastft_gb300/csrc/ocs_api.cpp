@@ -76,6 +76,12 @@ struct Context {
     std::mutex batch_mu;
     ocs::internal::BatchScratch batch;
     int batch_occ = 0;
+    // A captured batch replays its descriptor upload from the buffers it was
+    // captured with, so each capture gets its own: ocs_batch_prepare sets one
+    // set aside, the next captured ocs_batch_device takes it, and it is kept
+    // (with that graph's descriptors) until ocs_shutdown.
+    ocs::internal::BatchScratch* graph_next = nullptr;
+    std::vector<ocs::internal::BatchScratch*> graph_kept;
     // error word of the bounded waits in the tensor-core kernels: mapped host
     // memory, so the host reads it without a copy or a stream order
     int* h_err = nullptr;
@@ -779,7 +785,7 @@ int batch_enqueue(ocs_request* reqs, int count, cudaStream_t st, BatchScratch& b
     if (!bp.tiles.empty()) {
         const size_t bytes = batch_bytes(bp.descs.size(), bp.tiles.size());
         if (capturing && (b.host_cap < bytes || b.dev_cap < bytes))
-            return fail(OCS_ENOMEM, "batch buffers not prepared (call ocs_batch_prepare before capture)");
+            return fail(OCS_ENOMEM, "batch buffers not prepared (call ocs_batch_prepare before each capture)");
         rc = batch_scratch_grow(b, bytes);
         if (rc) return rc;
         const int occ = batch_occ_get();
@@ -826,7 +832,10 @@ extern "C" int ocs_batch_prepare(const ocs_request* reqs, int count)
     if (rc) return rc;
     Context& c = ctx();
     std::lock_guard<std::mutex> lk(c.batch_mu);
-    return ocs::internal::batch_prepare_into(reqs, count, c.batch);
+    rc = ocs::internal::batch_prepare_into(reqs, count, c.batch);
+    if (rc) return rc;
+    if (!c.graph_next) c.graph_next = new ocs::internal::BatchScratch();
+    return ocs::internal::batch_prepare_into(reqs, count, *c.graph_next);
 }
 
 extern "C" int ocs_batch_device(ocs_request* reqs, int count, void* stream)
@@ -834,9 +843,19 @@ extern "C" int ocs_batch_device(ocs_request* reqs, int count, void* stream)
     if (count < 0 || (count > 0 && !reqs)) return fail(OCS_EINVAL, "bad request list");
     int rc = ensure_init();
     if (rc) return rc;
+    const cudaStream_t st = (cudaStream_t)stream;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    OCS_CUDA(cudaStreamIsCapturing(st, &cap));
     Context& c = ctx();
     std::lock_guard<std::mutex> lk(c.batch_mu);
-    return ocs::internal::batch_enqueue(reqs, count, (cudaStream_t)stream, c.batch);
+    if (cap == cudaStreamCaptureStatusNone) return ocs::internal::batch_enqueue(reqs, count, st, c.batch);
+    if (!c.graph_next)
+        return fail(OCS_ENOMEM, "batch buffers not prepared (call ocs_batch_prepare before each capture)");
+    rc = ocs::internal::batch_enqueue(reqs, count, st, *c.graph_next);
+    if (rc) return rc;
+    c.graph_kept.push_back(c.graph_next);
+    c.graph_next = nullptr;
+    return OCS_OK;
 }
 
 namespace ocs {
@@ -880,6 +899,13 @@ void ocs_shutdown(void)
     c.free_slots.clear();
     c.occupancy.clear();
     ocs::internal::batch_scratch_release(c.batch);
+    if (c.graph_next) c.graph_kept.push_back(c.graph_next);
+    c.graph_next = nullptr;
+    for (auto* g : c.graph_kept) {
+        ocs::internal::batch_scratch_release(*g);
+        delete g;
+    }
+    c.graph_kept.clear();
     c.batch_occ = 0;
     if (c.h_err) cudaFreeHost(c.h_err);
     c.h_err = nullptr;

@@ -128,3 +128,56 @@ def test_batch_cuda_graph_capture(ocs_lib):
     torch.cuda.synchronize()
     for b, r in zip(bufs, ref):
         assert torch.equal(b[1], r)
+
+
+def _device_requests(ocs_lib, items):
+    import torch
+
+    bufs, reqs_in = [], []
+    for (x, exp, ov, opts) in items:
+        g = ocs_lib.geometry(x.size, exp, ov, opts)
+        d_in = torch.from_numpy(x).cuda()
+        d_out = torch.zeros(g.out_floats, device="cuda")
+        bufs.append((d_in, d_out))
+        reqs_in.append((d_in, x.size, exp, ov, opts, d_out, g.out_floats))
+    return bufs, ocs_lib.make_requests(reqs_in)
+
+
+def test_batch_graph_replays_its_own_requests(ocs_lib):
+    """A captured batch keeps its own descriptors: replayed after an eager
+    batch and a second capture have used the library's batch buffers, each
+    graph still computes exactly its own requests."""
+    import torch
+
+    ba, ra = _device_requests(ocs_lib, _mix(16, seed=5, exps=range(6, 14)))
+    bb, rb = _device_requests(ocs_lib, _mix(20, seed=6, exps=range(6, 14)))
+    assert all(s == 0 for s in ocs_lib.batch_device(ra))
+    assert all(s == 0 for s in ocs_lib.batch_device(rb))
+    torch.cuda.synchronize()
+    ref_a = [b[1].clone() for b in ba]
+    ref_b = [b[1].clone() for b in bb]
+    s = torch.cuda.Stream()
+    graphs = []
+    for reqs in (ra, rb):
+        ocs_lib.batch_prepare(reqs)  # once before each capture
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                ocs_lib.batch_device(reqs, s)
+        graphs.append(g)
+    for b in ba + bb:
+        b[1].zero_()
+    ocs_lib.batch_device(rb)  # an eager batch after both captures
+    torch.cuda.synchronize()
+    graphs[0].replay()
+    torch.cuda.synchronize()
+    assert all(torch.equal(b[1], r) for b, r in zip(ba, ref_a))
+    assert all(torch.equal(b[1], r) for b, r in zip(bb, ref_b))
+    for b in ba + bb:
+        b[1].zero_()
+    torch.cuda.synchronize()
+    graphs[1].replay()
+    graphs[0].replay()
+    torch.cuda.synchronize()
+    assert all(torch.equal(b[1], r) for b, r in zip(ba, ref_a))
+    assert all(torch.equal(b[1], r) for b, r in zip(bb, ref_b))
