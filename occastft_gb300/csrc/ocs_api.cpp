@@ -508,26 +508,28 @@ int launch_frames(const Request& r, const float* d_sig, uint64_t n, float* d_out
         cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
         cudaStreamIsCapturing(st, &cap);
         if (cap == cudaStreamCaptureStatusNone) {
-            cudaEvent_t e0, e1;
-            OCS_CUDA(cudaEventCreate(&e0));
-            OCS_CUDA(cudaEventCreate(&e1));
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            cudaError_t te = cudaEventCreate(&e0);
+            if (te == cudaSuccess) te = cudaEventCreate(&e1);
             float best = 1e30f;
-            for (int i = 0; i < nc; ++i) {
+            for (int i = 0; i < nc && te == cudaSuccess; ++i) {
                 const int v = cand[i];
-                OCS_CUDA(launch_variant(v, r, outk, a, tw_single, tw_pair, st));
-                OCS_CUDA(cudaEventRecord(e0, st));
-                for (int k = 0; k < 3; ++k) OCS_CUDA(launch_variant(v, r, outk, a, tw_single, tw_pair, st));
-                OCS_CUDA(cudaEventRecord(e1, st));
-                OCS_CUDA(cudaEventSynchronize(e1));
+                te = launch_variant(v, r, outk, a, tw_single, tw_pair, st);
+                if (te == cudaSuccess) te = cudaEventRecord(e0, st);
+                for (int k = 0; k < 3 && te == cudaSuccess; ++k)
+                    te = launch_variant(v, r, outk, a, tw_single, tw_pair, st);
+                if (te == cudaSuccess) te = cudaEventRecord(e1, st);
+                if (te == cudaSuccess) te = cudaEventSynchronize(e1);
                 float ms = 0.0f;
-                OCS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-                if (ms < best) {
+                if (te == cudaSuccess) te = cudaEventElapsedTime(&ms, e0, e1);
+                if (te == cudaSuccess && ms < best) {
                     best = ms;
                     choice = v;
                 }
             }
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
+            if (e0) cudaEventDestroy(e0);
+            if (e1) cudaEventDestroy(e1);
+            if (te != cudaSuccess) return cuda_fail(te, "kernel variant timing");
             Context& c = ctx();
             std::lock_guard<std::mutex> lk(c.mu);
             tune_store_locked(c, key, choice);
@@ -556,6 +558,18 @@ void out_range(const Request& r, uint64_t f0, uint64_t f1, uint64_t* off, uint64
     }
 }
 
+void destroy_slot(Slot* s)
+{
+    if (s->s_h2d) cudaStreamDestroy(s->s_h2d);
+    if (s->s_comp) cudaStreamDestroy(s->s_comp);
+    if (s->s_d2h) cudaStreamDestroy(s->s_d2h);
+    for (auto e : s->ev_in) cudaEventDestroy(e);
+    for (auto e : s->ev_comp) cudaEventDestroy(e);
+    if (s->d_in) cudaFree(s->d_in);
+    if (s->d_out) cudaFree(s->d_out);
+    delete s;
+}
+
 Slot* acquire_slot(int* rc)
 {
     Context& c = ctx();
@@ -573,16 +587,19 @@ Slot* acquire_slot(int* rc)
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->s_comp, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->s_d2h, cudaStreamNonBlocking);
     for (int i = 0; i < kMaxChunks && e == cudaSuccess; ++i) {
-        cudaEvent_t a, b;
+        cudaEvent_t a = nullptr, b = nullptr;
         e = cudaEventCreateWithFlags(&a, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b, cudaEventDisableTiming);
         if (e == cudaSuccess) {
             s->ev_in.push_back(a);
             s->ev_comp.push_back(b);
+        } else if (a) {
+            cudaEventDestroy(a);
         }
     }
     if (e != cudaSuccess) {
         *rc = cuda_fail(e, "slot creation");
+        destroy_slot(s);
         return nullptr;
     }
     std::lock_guard<std::mutex> lk(c.mu);
@@ -885,16 +902,7 @@ void ocs_shutdown(void)
     c.windows.clear();
     c.windows_host.clear();
     c.two_level.clear();
-    for (Slot* s : c.all_slots) {
-        cudaStreamDestroy(s->s_h2d);
-        cudaStreamDestroy(s->s_comp);
-        cudaStreamDestroy(s->s_d2h);
-        for (auto e : s->ev_in) cudaEventDestroy(e);
-        for (auto e : s->ev_comp) cudaEventDestroy(e);
-        if (s->d_in) cudaFree(s->d_in);
-        if (s->d_out) cudaFree(s->d_out);
-        delete s;
-    }
+    for (Slot* s : c.all_slots) destroy_slot(s);
     c.all_slots.clear();
     c.free_slots.clear();
     c.occupancy.clear();
