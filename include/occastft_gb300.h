@@ -177,6 +177,8 @@ typedef struct ocs_server_config {
 typedef struct ocs_server_stats {
     uint64_t completed, failed, rejected, pending, batches, samples;
     double elapsed_ms; /* since start or the last reset */
+    /* p50/p99/p999 over the most recent 2^20 completed requests; max over
+     * all completed since start or the last reset */
     double p50_ms, p99_ms, p999_ms, max_ms;
     uint64_t pool_bytes, pool_used;
 } ocs_server_stats;
@@ -184,7 +186,10 @@ typedef struct ocs_server_stats {
 int ocs_server_start(const ocs_server_config* cfg);
 /* Queues one request; in/out are host buffers that must stay valid until
  * ocs_server_wait returns (pinned buffers copy fastest).  Fails with
- * OCS_ENOMEM when the request alone exceeds the device pool. */
+ * OCS_ENOMEM when the request alone exceeds the device pool.  A request
+ * whose copy to or from the device cannot be issued finishes with status
+ * OCS_ECUDA.  The server calls may run on any threads, including a stop
+ * while other threads submit or wait. */
 int ocs_server_submit(const float* in, uint64_t n, int window_size_exp, float overlap_ratio, const char* options,
                       float* out, uint64_t out_cap, uint64_t* ticket);
 /* Waits up to timeout_ms (< 0: no limit) for a request; *status is its result. */

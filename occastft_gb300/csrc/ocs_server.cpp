@@ -135,11 +135,41 @@ struct Server {
     // statistics
     double t_start = 0.0;
     uint64_t completed = 0, failed = 0, rejected = 0, samples = 0, batches = 0;
-    std::vector<double> lat_ms;
+    std::vector<double> lat_ms;  // ring of the most recent kLatencyWindow latencies
+    size_t lat_next = 0;
+    double lat_max = 0.0;
 };
 
-Server* g_srv = nullptr;
-std::mutex g_srv_mu;
+constexpr size_t kLatencyWindow = size_t(1) << 20;
+
+// The running server.  Calls take a reference under g_ptr_mu, so a stop
+// that runs meanwhile never frees a server another call is still using;
+// g_life_mu keeps starts and stops one at a time.  The holder is never
+// destroyed: a server still running at process exit is left alone rather
+// than destroyed with its worker thread attached.
+std::shared_ptr<Server>& g_srv = *new std::shared_ptr<Server>();
+std::mutex g_ptr_mu;
+std::mutex g_life_mu;
+
+std::shared_ptr<Server> current()
+{
+    std::lock_guard<std::mutex> g(g_ptr_mu);
+    return g_srv;
+}
+
+// Frees the slots' streams and scratch and the device pool (no worker running).
+void release_resources(Server& S)
+{
+    for (auto& s : S.slots) {
+        if (!s->st) continue;
+        cudaStreamSynchronize(s->st);
+        ocs::internal::batch_scratch_release(s->scratch);
+        cudaStreamDestroy(s->st);
+        s->st = nullptr;
+    }
+    if (S.d_pool) cudaFree(S.d_pool);
+    S.d_pool = nullptr;
+}
 
 int err(int code, const std::string& m)
 {
@@ -170,7 +200,14 @@ void reap(Server& S)
             if (j->status == OCS_OK) {
                 ++S.completed;
                 S.samples += j->n;
-                S.lat_ms.push_back(j->t_done - j->t_submit);
+                const double ms = j->t_done - j->t_submit;
+                if (S.lat_ms.size() < kLatencyWindow) {
+                    S.lat_ms.push_back(ms);
+                } else {
+                    S.lat_ms[S.lat_next] = ms;
+                    S.lat_next = (S.lat_next + 1) % kLatencyWindow;
+                }
+                S.lat_max = std::max(S.lat_max, ms);
             } else {
                 ++S.failed;
             }
@@ -182,22 +219,38 @@ void reap(Server& S)
     }
 }
 
+// A request whose copy to or from the device cannot be issued fails with
+// OCS_ECUDA; the copy's error is cleared so the batch launch does not take it
+// for its own.
 void issue(Server& S, Slot& s)
 {
-    std::vector<ocs_request> reqs(s.jobs.size());
+    std::vector<ocs_request> reqs;
+    std::vector<size_t> job_of;  // s.jobs index of each request
+    reqs.reserve(s.jobs.size());
+    job_of.reserve(s.jobs.size());
     for (size_t i = 0; i < s.jobs.size(); ++i) {
         Job& j = *s.jobs[i];
         float* din = reinterpret_cast<float*>(S.d_pool + j.in_off);
         float* dout = reinterpret_cast<float*>(S.d_pool + j.out_off);
-        cudaMemcpyAsync(din, j.in, j.n * 4, cudaMemcpyHostToDevice, s.st);
-        reqs[i] = ocs_request{din, j.n, j.exp, j.ov, j.options.c_str(), dout, j.out_floats, -1, 0};
+        if (cudaMemcpyAsync(din, j.in, j.n * 4, cudaMemcpyHostToDevice, s.st) != cudaSuccess) {
+            cudaGetLastError();
+            j.status = OCS_ECUDA;
+            continue;
+        }
+        reqs.push_back(ocs_request{din, j.n, j.exp, j.ov, j.options.c_str(), dout, j.out_floats, -1, 0});
+        job_of.push_back(i);
     }
-    int rc = ocs::internal::batch_enqueue(reqs.data(), (int)reqs.size(), s.st, s.scratch);
-    for (size_t i = 0; i < s.jobs.size(); ++i) {
-        Job& j = *s.jobs[i];
-        j.status = rc ? rc : reqs[i].status;
-        if (j.status == OCS_OK)
-            cudaMemcpyAsync(j.out, S.d_pool + j.out_off, j.out_floats * 4, cudaMemcpyDeviceToHost, s.st);
+    const int rc =
+        reqs.empty() ? OCS_OK : ocs::internal::batch_enqueue(reqs.data(), (int)reqs.size(), s.st, s.scratch);
+    for (size_t k = 0; k < reqs.size(); ++k) {
+        Job& j = *s.jobs[job_of[k]];
+        j.status = rc ? rc : reqs[k].status;
+        if (j.status == OCS_OK &&
+            cudaMemcpyAsync(j.out, S.d_pool + j.out_off, j.out_floats * 4, cudaMemcpyDeviceToHost, s.st) !=
+                cudaSuccess) {
+            cudaGetLastError();
+            j.status = OCS_ECUDA;
+        }
     }
     if (cudaLaunchHostFunc(s.st, on_slot_done, &s) != cudaSuccess) {
         cudaStreamSynchronize(s.st);
@@ -252,11 +305,11 @@ extern "C" {
 
 int ocs_server_start(const ocs_server_config* cfg)
 {
-    std::lock_guard<std::mutex> g(g_srv_mu);
-    if (g_srv) return err(OCS_EINVAL, "server already running");
+    std::lock_guard<std::mutex> g(g_life_mu);
+    if (current()) return err(OCS_EINVAL, "server already running");
     int rc = ocs::internal::ensure_ready();
     if (rc) return rc;
-    auto S = std::make_unique<Server>();
+    auto S = std::make_shared<Server>();
     cudaGetDevice(&S->device);
     size_t fr = 0, tot = 0;
     cudaMemGetInfo(&fr, &tot);
@@ -273,22 +326,23 @@ int ocs_server_start(const ocs_server_config* cfg)
         auto s = std::make_unique<Slot>();
         s->srv = S.get();
         if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess) {
+            release_resources(*S);
             return err(OCS_ECUDA, "stream creation failed");
         }
         S->slots.push_back(std::move(s));
     }
     S->running = true;
     S->t_start = now_ms();
-    Server* raw = S.get();
-    S->worker = std::thread(worker_main, raw);
-    g_srv = S.release();
+    S->worker = std::thread(worker_main, S.get());
+    std::lock_guard<std::mutex> p(g_ptr_mu);
+    g_srv = S;
     return OCS_OK;
 }
 
 int ocs_server_submit(const float* in, uint64_t n, int window_size_exp, float overlap_ratio, const char* options,
                       float* out, uint64_t out_cap, uint64_t* ticket)
 {
-    Server* S = g_srv;
+    const std::shared_ptr<Server> S = current();
     if (!S) return err(OCS_EINVAL, "server not running");
     if (!in || !out || !ticket) return err(OCS_EINVAL, "null argument");
     ocs_geometry g;
@@ -323,7 +377,7 @@ int ocs_server_submit(const float* in, uint64_t n, int window_size_exp, float ov
 
 int ocs_server_wait(uint64_t ticket, int timeout_ms, int* status)
 {
-    Server* S = g_srv;
+    const std::shared_ptr<Server> S = current();
     if (!S) return err(OCS_EINVAL, "server not running");
     std::unique_lock<std::mutex> lk(S->mu);
     auto it = S->jobs.find(ticket);
@@ -339,7 +393,7 @@ int ocs_server_wait(uint64_t ticket, int timeout_ms, int* status)
 
 int ocs_server_cancel(uint64_t ticket)
 {
-    Server* S = g_srv;
+    const std::shared_ptr<Server> S = current();
     if (!S) return err(OCS_EINVAL, "server not running");
     std::lock_guard<std::mutex> lk(S->mu);
     auto it = S->jobs.find(ticket);
@@ -355,46 +409,52 @@ int ocs_server_cancel(uint64_t ticket)
 
 int ocs_server_get_stats(ocs_server_stats* out)
 {
-    Server* S = g_srv;
+    const std::shared_ptr<Server> S = current();
     if (!S || !out) return err(OCS_EINVAL, "server not running");
-    std::lock_guard<std::mutex> lk(S->mu);
-    std::memset(out, 0, sizeof(*out));
-    out->completed = S->completed;
-    out->failed = S->failed;
-    out->rejected = S->rejected;
-    out->pending = S->pending.size();
-    out->batches = S->batches;
-    out->samples = S->samples;
-    out->elapsed_ms = now_ms() - S->t_start;
-    out->pool_bytes = S->pool.capacity();
-    out->pool_used = S->pool.used();
-    std::vector<double> l = S->lat_ms;
+    std::vector<double> l;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        std::memset(out, 0, sizeof(*out));
+        out->completed = S->completed;
+        out->failed = S->failed;
+        out->rejected = S->rejected;
+        out->pending = S->pending.size();
+        out->batches = S->batches;
+        out->samples = S->samples;
+        out->elapsed_ms = now_ms() - S->t_start;
+        out->pool_bytes = S->pool.capacity();
+        out->pool_used = S->pool.used();
+        out->max_ms = S->lat_max;
+        l = S->lat_ms;
+    }
     if (!l.empty()) {
+        // sorted outside the lock, so the worker is not held up
         std::sort(l.begin(), l.end());
         auto q = [&](double p) { return l[std::min(l.size() - 1, (size_t)(p * (l.size() - 1) + 0.5))]; };
         out->p50_ms = q(0.50);
         out->p99_ms = q(0.99);
         out->p999_ms = q(0.999);
-        out->max_ms = l.back();
     }
     return OCS_OK;
 }
 
 int ocs_server_reset_stats(void)
 {
-    Server* S = g_srv;
+    const std::shared_ptr<Server> S = current();
     if (!S) return err(OCS_EINVAL, "server not running");
     std::lock_guard<std::mutex> lk(S->mu);
     S->completed = S->failed = S->rejected = S->samples = S->batches = 0;
     S->lat_ms.clear();
+    S->lat_next = 0;
+    S->lat_max = 0.0;
     S->t_start = now_ms();
     return OCS_OK;
 }
 
 int ocs_server_stop(void)
 {
-    std::lock_guard<std::mutex> g(g_srv_mu);
-    Server* S = g_srv;
+    std::lock_guard<std::mutex> g(g_life_mu);
+    const std::shared_ptr<Server> S = current();
     if (!S) return err(OCS_EINVAL, "server not running");
     {
         std::lock_guard<std::mutex> lk(S->mu);
@@ -402,14 +462,9 @@ int ocs_server_stop(void)
         S->cv_work.notify_all();
     }
     S->worker.join();
-    for (auto& s : S->slots) {
-        cudaStreamSynchronize(s->st);
-        ocs::internal::batch_scratch_release(s->scratch);
-        cudaStreamDestroy(s->st);
-    }
-    cudaFree(S->d_pool);
-    g_srv = nullptr;
-    delete S;
+    release_resources(*S);
+    std::lock_guard<std::mutex> p(g_ptr_mu);
+    g_srv.reset();
     return OCS_OK;
 }
 
