@@ -11,7 +11,10 @@
 #include <algorithm>
 #include <cctype>
 #include <cstring>
+#include <exception>
+#include <memory>
 #include <mutex>
+#include <new>
 #include <set>
 #include <thread>
 
@@ -248,8 +251,25 @@ void WsServer::stop()
 
 void WsServer::run(const Handler& on_message)
 {
-    std::vector<std::thread> threads;
+    // connection threads, joined as they finish so a long-running server
+    // does not accumulate them
+    struct Worker {
+        std::thread t;
+        std::shared_ptr<std::atomic<bool>> done;
+    };
+    std::vector<Worker> workers;
+    auto reap = [&workers] {
+        for (auto it = workers.begin(); it != workers.end();) {
+            if (it->done->load()) {
+                it->t.join();
+                it = workers.erase(it);
+            } else {
+                ++it;
+            }
+        }
+    };
     while (!stopping_) {
+        reap();
         pollfd p{lfd_, POLLIN, 0};
         const int r = ::poll(&p, 1, 100);
         if (r <= 0 || !(p.revents & POLLIN)) continue;
@@ -261,11 +281,24 @@ void WsServer::run(const Handler& on_message)
             std::lock_guard<std::mutex> lk(g_conn_mu);
             g_conns.insert(fd);
         }
-        threads.emplace_back([this, fd, &on_message] { serve(fd, on_message); });
+        auto done = std::make_shared<std::atomic<bool>>(false);
+        try {
+            workers.push_back(Worker{std::thread([this, fd, &on_message, done] {
+                                         serve(fd, on_message);
+                                         done->store(true);
+                                     }),
+                                     done});
+        } catch (const std::exception&) {  // no thread for it: drop the connection
+            {
+                std::lock_guard<std::mutex> lk(g_conn_mu);
+                g_conns.erase(fd);
+            }
+            ::close(fd);
+        }
     }
     ::close(lfd_);
     lfd_ = -1;
-    for (auto& t : threads) t.join();
+    for (auto& w : workers) w.t.join();
 }
 
 void WsServer::serve(int fd, const Handler& on_message)
@@ -321,12 +354,22 @@ void WsServer::serve(int fd, const Handler& on_message)
             } else if (op != 0 || !in_msg) {
                 break;
             }
-            if (have + len > kMaxMessage) {
+            // have <= kMaxMessage here, so the subtraction cannot wrap (a sum
+            // with a 64-bit frame length could); an allocation the host
+            // cannot make is answered like a message that is too big
+            bool fits = len <= kMaxMessage && have <= kMaxMessage - len;
+            if (fits) {
+                try {
+                    msg.store.resize((have + len + 7) / 8);
+                } catch (const std::bad_alloc&) {
+                    fits = false;
+                }
+            }
+            if (!fits) {
                 const uint8_t code[2] = {0x03, 0xF1};  // 1009 message too big
                 conn.send_frame(8, code, 2);
                 break;
             }
-            msg.store.resize((have + len + 7) / 8);
             uint8_t* dst = reinterpret_cast<uint8_t*>(msg.store.data()) + have;
             if (len && !recv_all(fd, dst, (size_t)len)) break;
             // unmask; the key repeats every 4 bytes of the frame payload
@@ -345,7 +388,13 @@ void WsServer::serve(int fd, const Handler& on_message)
             if (fin) {
                 msg.size = (size_t)have;
                 in_msg = false;
-                on_message(conn, msg);
+                try {
+                    on_message(conn, msg);
+                } catch (const std::exception&) {  // the handler failed: end this connection only
+                    const uint8_t code[2] = {0x03, 0xF3};  // 1011 internal error
+                    conn.send_frame(8, code, 2);
+                    break;
+                }
                 msg = Message{};
             }
         }

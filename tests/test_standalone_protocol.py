@@ -134,6 +134,27 @@ def test_ping_and_close_frames(runner):
     ws.close()
 
 
+@pytest.mark.parametrize("length", [2**64 - 5, 2**63, 2**37])
+def test_oversized_continuation_frame_is_refused(runner, length):
+    """A continuation frame whose 64-bit length is above the message limit
+    (including lengths whose sum with the bytes already received would wrap,
+    and ones with the most significant bit set, which RFC 6455 5.2 forbids)
+    is answered with close code 1009 before any payload is stored; the runner
+    keeps serving other connections."""
+    _, port = runner
+    ws = proxy.WsClient("127.0.0.1", port)
+    mask = b"\x01\x02\x03\x04"
+    first = bytes(range(10))
+    ws.sock.sendall(bytes([0x02, 0x80 | len(first)]) + mask + bytes(b ^ mask[i & 3] for i, b in enumerate(first)))
+    ws.sock.sendall(bytes([0x80, 0x80 | 127]) + struct.pack(">Q", length) + mask + bytes(64))
+    assert ws.recv(timeout=30) == (8, struct.pack(">H", 1009))
+    ws.close()
+    other = proxy.WsClient("127.0.0.1", port)
+    other.ping(b"still serving")
+    assert other.recv(timeout=30) == (10, b"still serving")
+    other.close()
+
+
 def test_close_request_stops_runner():
     p, port = cu.start_cudarun()
     try:
