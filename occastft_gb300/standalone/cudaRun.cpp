@@ -108,7 +108,7 @@ void handle_request(Connection& c, const Message& m)
         } else {
             ShmMapping map;
             status = shm_map(q.sharedMemory, q.overlapdataLength, map, g_shm_mode == ShmMode::populate);
-            if (status.empty() && q.dataLength * sizeof(float) > map.bytes)
+            if (status.empty() && q.dataLength > map.bytes / sizeof(float))
                 status = "dataLength floats exceed the shared memory region";
             bool pinned = false;
             if (status.empty() && g_shm_mode == ShmMode::pin)

@@ -7,6 +7,7 @@
 #include <unistd.h>
 
 #include <cerrno>
+#include <cstdint>
 #include <cstring>
 
 namespace ocs_standalone {
@@ -14,6 +15,7 @@ namespace ocs_standalone {
 size_t page_rounded_bytes(uint64_t floats)
 {
     const uint64_t page = (uint64_t)sysconf(_SC_PAGESIZE);
+    if (floats > (UINT64_MAX - page) / sizeof(float)) return 0;  // no such region: refused by the caller
     const uint64_t bytes = floats * sizeof(float);
     return (size_t)((bytes + page - 1) / page * page);
 }
@@ -22,7 +24,7 @@ std::string shm_map(const std::string& name, uint64_t overlap_floats, ShmMapping
 {
     m = ShmMapping{};
     const size_t bytes = page_rounded_bytes(overlap_floats);
-    if (bytes == 0) return "shared memory region of zero bytes";
+    if (bytes == 0) return "shared memory region of zero bytes or beyond the address space";
     const int fd = shm_open(name.c_str(), O_RDWR, 0666);
     if (fd < 0) return "shm_open " + name + ": " + std::strerror(errno);
     // the mapping must not reach past the object: a store there would fault
