@@ -156,9 +156,10 @@ int ocs_batch_device(ocs_request* reqs, int count, void* stream);
  * distinct window tables of one call within the array's window region.
  * Requests with larger windows get status OCS_EINVAL.  The first call on a
  * device (with that device current) sets the array up and synchronizes
- * `stream` once; make it before any stream capture.  All calls share the
- * array: calls whose work overlaps on the GPU race, so order them on one
- * stream or with events. */
+ * `stream` once.  Calls cannot be captured into a CUDA graph (OCS_EINVAL):
+ * their descriptors go through a host staging buffer that every call
+ * rewrites.  All calls share the array: calls whose work overlaps on the GPU
+ * race, so order them on one stream or with events. */
 int ocs_batch_device_noalloc(ocs_request* reqs, int count, void* stream);
 
 /* ---- serving: a continuous-batching request server ----

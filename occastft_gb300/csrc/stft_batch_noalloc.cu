@@ -24,8 +24,12 @@
 //
 // Set-up: the first call on a device (with that device current) takes the
 // array's device address with cudaGetSymbolAddress, fills the twiddle tables
-// of every supported window size into it and waits for that to finish.  Make
-// that first call before any stream capture.
+// of every supported window size into it and waits for that to finish.
+//
+// Calls are not capturable into a CUDA graph (refused with OCS_EINVAL): a
+// replay would upload whatever descriptors the host staging buffer holds
+// then, which every later call rewrites.  ocs_batch_device is the capturable
+// batch entry point.
 //
 // Sharing: every call uses the same array and leaves its contents behind.
 // The call rewrites the descriptors and resets the tile counter to zero each
@@ -229,8 +233,15 @@ extern "C" int ocs_batch_device_noalloc(ocs_request* reqs, int count, void* stre
         return fail(OCS_ENOMEM, "no-allocation batch: more than " + std::to_string(kMaxRequests) +
                                     " requests in one call");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // A captured call would replay its descriptor upload from the host
+    // staging buffer, which every later call rewrites: refused.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaError_t ce = cudaStreamIsCapturing(st, &cap);
+    if (ce != cudaSuccess) return fail(OCS_ECUDA, cudaGetErrorString(ce));
+    if (cap != cudaStreamCaptureStatusNone)
+        return fail(OCS_EINVAL, "no-allocation batch: calls cannot be captured into a CUDA graph");
     int dev = 0;
-    cudaError_t ce = cudaGetDevice(&dev);
+    ce = cudaGetDevice(&dev);
     if (ce != cudaSuccess) return fail(OCS_ECUDA, cudaGetErrorString(ce));
     if (dev < 0 || dev >= kMaxDevices) return fail(OCS_EINVAL, "device index out of range");
     std::lock_guard<std::mutex> lk(g_mu);
