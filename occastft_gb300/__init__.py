@@ -154,6 +154,24 @@ def _stream_handle(stream) -> Optional[int]:
     return getattr(stream, "cuda_stream", stream)
 
 
+def _device_ptr(buf, count: int, what: str) -> int:
+    """Device address of a pointer argument.  A torch tensor must be a CUDA,
+    contiguous float32 tensor of at least `count` elements (a host tensor or a
+    short one would turn into an illegal address on the GPU); a plain integer
+    address is the caller's responsibility and passes unchecked."""
+    if not hasattr(buf, "data_ptr"):
+        return int(buf)
+    if not getattr(buf, "is_cuda", False):
+        raise OcsError(OCS_EINVAL, f"{what}: the tensor is not on a CUDA device")
+    if str(buf.dtype) != "torch.float32":
+        raise OcsError(OCS_EINVAL, f"{what}: tensor of {buf.dtype}, float32 expected")
+    if not buf.is_contiguous():
+        raise OcsError(OCS_EINVAL, f"{what}: the tensor is not contiguous")
+    if buf.numel() < count:
+        raise OcsError(OCS_EINVAL, f"{what}: the tensor holds {buf.numel()} floats, {count} needed")
+    return buf.data_ptr()
+
+
 def activate(signal: np.ndarray, window_size_exp: int, overlap_ratio: float, options: str = DEFAULT_OPTIONS,
              out: Optional[np.ndarray] = None) -> np.ndarray:
     """Host buffers in and out (ActivateSTFT semantics); raises OcsError on failure."""
@@ -161,6 +179,10 @@ def activate(signal: np.ndarray, window_size_exp: int, overlap_ratio: float, opt
     g = geometry(x.size, window_size_exp, overlap_ratio, options)
     if out is None:
         out = np.empty(g.out_floats, dtype=np.float32)
+    elif not (isinstance(out, np.ndarray) and out.dtype == np.float32 and out.flags.c_contiguous
+              and out.flags.writeable):
+        # the native call writes out.size float32 values at out's address
+        raise OcsError(OCS_EINVAL, "out must be a writable C-contiguous float32 numpy array")
     n_out = ctypes.c_uint64(0)
     _check(lib().ocs_activate(x.ctypes.data, x.size, window_size_exp, overlap_ratio, options.encode(),
                               out.ctypes.data, out.size, ctypes.byref(n_out)))
@@ -170,8 +192,8 @@ def activate(signal: np.ndarray, window_size_exp: int, overlap_ratio: float, opt
 def activate_device(d_in, n: int, window_size_exp: int, overlap_ratio: float, options: str, d_out,
                     out_cap: int, stream=None) -> None:
     """Device-resident pipeline (pointers as ints or torch tensors), asynchronous on `stream`."""
-    pin = d_in.data_ptr() if hasattr(d_in, "data_ptr") else int(d_in)
-    pout = d_out.data_ptr() if hasattr(d_out, "data_ptr") else int(d_out)
+    pin = _device_ptr(d_in, n, "input")
+    pout = _device_ptr(d_out, out_cap, "output")
     _check(lib().ocs_activate_device(pin, n, window_size_exp, overlap_ratio, options.encode(), pout, out_cap,
                                      _stream_handle(stream)))
 
@@ -207,12 +229,12 @@ def make_requests(items):
     for i, (din, n, exp, ov, opts, dout, cap) in enumerate(items):
         ob = opts.encode()
         keep.append(ob)
-        arr[i].in_ = din.data_ptr() if hasattr(din, "data_ptr") else int(din)
+        arr[i].in_ = _device_ptr(din, n, f"request {i} input")
         arr[i].n = n
         arr[i].window_size_exp = exp
         arr[i].overlap_ratio = ov
         arr[i].options = ob
-        arr[i].out = dout.data_ptr() if hasattr(dout, "data_ptr") else int(dout)
+        arr[i].out = _device_ptr(dout, cap, f"request {i} output")
         arr[i].out_cap = cap
         arr[i].status = -1
     arr._keep = keep  # the option strings must outlive the array
@@ -323,7 +345,8 @@ class runnerFunction:  # noqa: N801 (reference namespace name)
 
     @staticmethod
     def _p(t):
-        return t.data_ptr() if hasattr(t, "data_ptr") else int(t)
+        # tensors: CUDA, float32, contiguous (sizes are the stage's own arguments)
+        return _device_ptr(t, 0, "stage buffer")
 
     @classmethod
     def Overlap(cls, origin, OFullSize, FullSize, windowSizeEXP, OMove, Realout, stream=None):  # noqa: N802,N803

@@ -119,3 +119,55 @@ def test_window_exponent_limits(ocs_lib):
     assert g.n_window == 1 << 22 and g.out_floats == g.qt * (1 << 22)
     with pytest.raises(ocs_lib.OcsError, match="above 2\\^22"):
         ocs_lib.geometry(50_000_000, 23, 0.5, "")
+
+
+def test_python_pointer_arguments_are_checked(ocs_lib):
+    """Tensors handed to the device-pointer calls are checked on the host
+    before any native call: a host tensor, another dtype, a strided view or a
+    buffer shorter than the stated size would otherwise become an illegal
+    address (or a wrong reading) on the GPU.  Raw integer addresses pass."""
+    import torch
+
+    cases = [(torch.zeros(64), "not on a CUDA device")]
+    for t, why in cases:
+        with pytest.raises(ocs_lib.OcsError, match=why):
+            ocs_lib.activate_device(t, 64, 6, 0.5, "", 0, 64)
+        with pytest.raises(ocs_lib.OcsError, match=why):
+            ocs_lib.make_requests([(t, 64, 6, 0.5, "", 0, 64)])
+        with pytest.raises(ocs_lib.OcsError, match=why):
+            ocs_lib.runnerFunction.ToPower(t, 0, 0, 64)
+
+    class Fake:  # stands in for a CUDA tensor on a machine without one
+        def __init__(self, dtype="torch.float32", contiguous=True, numel=64):
+            self.is_cuda, self.dtype, self._c, self._n = True, dtype, contiguous, numel
+
+        def data_ptr(self):
+            return 0x10000
+
+        def is_contiguous(self):
+            return self._c
+
+        def numel(self):
+            return self._n
+
+    assert ocs_lib._device_ptr(Fake(), 64, "x") == 0x10000
+    assert ocs_lib._device_ptr(0x2000, 1 << 40, "x") == 0x2000
+    for fake, why in [(Fake(dtype="torch.float64"), "float32 expected"), (Fake(contiguous=False), "not contiguous"),
+                      (Fake(numel=63), "63 floats, 64 needed")]:
+        with pytest.raises(ocs_lib.OcsError, match=why):
+            ocs_lib._device_ptr(fake, 64, "x")
+        with pytest.raises(ocs_lib.OcsError, match=why):
+            ocs_lib.make_requests([(fake, 64, 6, 0.5, "", 0x3000, 64)])
+
+
+def test_activate_out_argument_is_checked(ocs_lib):
+    """ocs_activate writes out.size float32 values at out's address: an out
+    array of another dtype, read-only or strided is refused first."""
+    x = signal(3, 1000)
+    for out in (np.zeros(10000, np.int8), np.zeros(10000, np.float64), np.zeros(20000, np.float32)[::2]):
+        with pytest.raises(ocs_lib.OcsError, match="float32 numpy array"):
+            ocs_lib.activate(x, 6, 0.5, "", out=out)
+    ro = np.zeros(10000, np.float32)
+    ro.flags.writeable = False
+    with pytest.raises(ocs_lib.OcsError, match="float32 numpy array"):
+        ocs_lib.activate(x, 6, 0.5, "", out=ro)
