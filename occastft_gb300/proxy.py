@@ -249,11 +249,21 @@ class STFTProxy:
         self.counter = 0
         self._runtime_fallback()
 
+    def _reap_runner(self):
+        """Ends and waits for the runner this proxy launched, so a runner
+        that a fallback leaves behind is not left running or unreaped."""
+        if self.runner is not None:
+            if self.runner.poll() is None:
+                self.runner.kill()
+            self.runner.wait()
+            self.runner = None
+
     # RuntimeFallback / TryConnect (STFTProxy.cpp:83-154)
     def _runtime_fallback(self):
         if self.ws is not None:
             self.ws.close()
             self.ws = None
+        self._reap_runner()
         while self.status == "OK":
             if not self.fallback:
                 self.status = "Run Out Fallback"
@@ -283,6 +293,7 @@ class STFTProxy:
                 return True
             except OSError:
                 time.sleep(0.5)
+        self._reap_runner()  # launched but never reachable
         return False
 
     def request_stft(self, data, window_size_exp: int, overlap_rate: float = 0.5,

@@ -70,3 +70,26 @@ def test_shared_memory_is_unlinked(tmp_path):
         assert set(os.listdir("/dev/shm")) - before == set()
     finally:
         p.kill_runner()
+
+
+def test_unreachable_runner_is_not_left_running(tmp_path, orc):
+    """A runner executable that starts but never accepts connections is given
+    up after the connection attempts, and the proxy ends that process before
+    moving on to the next runtime of the list."""
+    (tmp_path / "dead").mkdir()
+    (tmp_path / "ok").mkdir()
+    pidfile = tmp_path / "pid"
+    exe = tmp_path / "dead" / "serialRun"
+    exe.write_text(f"#!/bin/sh\necho $$ > {pidfile}\nexec sleep 600\n")
+    exe.chmod(exe.stat().st_mode | stat.S_IEXEC)
+    d2 = make_serial_runner(str(tmp_path / "ok"))
+    p = proxy.STFTProxy([("SERIAL", str(tmp_path / "dead")), ("SERIAL", d2)])
+    try:
+        assert p.status == "OK" and p.gpu_type == "SERIAL"
+        pid = int(pidfile.read_text())
+        assert not os.path.exists(f"/proc/{pid}") or open(f"/proc/{pid}/stat").read().split()[2] == "Z"
+        x = signal(6, 8000)
+        assert np.array_equal(p.request_stft(x, 8, 0.5, "--hamming_window"),
+                              orc.serial_pipeline(x, 8, 0.5, "--hamming_window"))
+    finally:
+        p.kill_runner()
