@@ -25,6 +25,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -150,6 +151,23 @@ def algorithmic_bytes(n: int, geo, half_complex: bool, dense: bool) -> int:
     N = geo.n_window
     read = min(n, (geo.frames - 1) * geo.hop + N) * 4
     return int(read + geo.out_floats * 4)
+
+
+FP32_LANES_PER_SM = 128       # FP32 FMA lanes per Blackwell SM
+NOMINAL_SM_MAX_MHZ = 2070.0   # GB300 maximum SM clock, used when none was sampled
+
+
+def fp32_pipe_bound(n_window: int, frames: int, seconds: float, sms: int, sm_mhz: float) -> dict:
+    """FP32-pipe bound of the plain form, reported beside the HBM one: a
+    real-input N-point FFT counted as 5*(N/2)*log2(N/2) flops per frame (the
+    complex half-length FFT; the O(N) untangle, window and magnitude are left
+    out), against the nominal FMA rate of `sms` SMs at `sm_mhz`."""
+    half = n_window / 2
+    flops = 5.0 * half * math.log2(half) * frames
+    peak = sms * FP32_LANES_PER_SM * 2.0 * sm_mhz * 1e6
+    achieved = flops / seconds
+    return {"gflop_s": round(achieved / 1e9, 1), "peak_gflop_s": round(peak / 1e9, 1),
+            "frac": round(achieved / peak, 4)}
 
 
 def load_peaks():
@@ -744,6 +762,8 @@ def run_ours(args):
     # the rest of the config: window sweep, device-resident
     sweep = []
     if rank == 0 and not args.no_sweep:
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        pipe_mhz = clk.get("sm_max_mhz") or NOMINAL_SM_MAX_MHZ
         for exp in range(6, 23):
             for wname in ("hamming", "blackman"):
                 for out_kind in ("power", "half_complex"):
@@ -756,7 +776,8 @@ def run_ours(args):
                     b = algorithmic_bytes(n, g, out_kind == "half_complex", False)
                     sweep.append({"N": 1 << exp, "window": wname, "output": out_kind,
                                   "gsamples_s": round(n / dt / 1e9, 2), "ms": round(dt * 1e3, 4),
-                                  "hbm_frac": round(b / dt / 1e9 / peak, 3)})
+                                  "hbm_frac": round(b / dt / 1e9 / peak, 3),
+                                  "fp32_pipe": fp32_pipe_bound(g.n_window, g.frames, dt, sms, pipe_mhz)})
 
     # cuFFT reference point (same GPU): batched R2C over pre-framed data
     cufft = None

@@ -1,0 +1,36 @@
+"""bench.py's host-side arithmetic, on CPU: the algorithmic bytes behind the
+roofline fraction and the FP32-pipe bound reported beside it."""
+import math
+
+import pytest
+
+import bench
+
+
+class _Geo:
+    def __init__(self, n_window, hop, frames, out_floats):
+        self.n_window, self.hop, self.frames, self.out_floats = n_window, hop, frames, out_floats
+
+
+def test_algorithmic_bytes_counts_covered_samples_and_output(ocs_lib):
+    g = ocs_lib.geometry(100_000_000, 10, 0.5, "--hamming_window")
+    # every sample is read once (the last frame runs past the end), every output float written once
+    assert bench.algorithmic_bytes(100_000_000, g, False, False) == 4 * 100_000_000 + 4 * g.out_floats
+    # a compat half-complex request computes only the frames its output needs
+    short = _Geo(1024, 512, 10, 10 * 1024)
+    assert bench.algorithmic_bytes(1_000_000, short, True, False) == 4 * (9 * 512 + 1024) + 4 * 10 * 1024
+
+
+def test_fp32_pipe_bound():
+    # 5 (N/2) log2(N/2) flops per frame against lanes x 2 x clock per SM
+    r = bench.fp32_pipe_bound(1024, 1000, 1e-3, 152, 2000.0)
+    flops = 5 * 512 * 9 * 1000
+    peak = 152 * bench.FP32_LANES_PER_SM * 2 * 2000e6
+    assert r["gflop_s"] == round(flops / 1e-3 / 1e9, 1)
+    assert r["peak_gflop_s"] == round(peak / 1e9, 1)
+    assert r["frac"] == pytest.approx(flops / 1e-3 / peak, abs=1e-4)
+    # doubling the window at a fixed frame count adds one radix-2 level
+    a = bench.fp32_pipe_bound(1024, 10**6, 1e-3, 152, 2000.0)
+    b = bench.fp32_pipe_bound(2048, 10**6, 1e-3, 152, 2000.0)
+    assert b["gflop_s"] / a["gflop_s"] == pytest.approx(2 * 10 / 9, rel=1e-6)
+    assert math.isclose(bench.NOMINAL_SM_MAX_MHZ, 2070.0)
