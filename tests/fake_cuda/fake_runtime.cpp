@@ -1,13 +1,14 @@
-// TEST INFRASTRUCTURE ONLY: the host-only CUDA stand-in and the library
-// internals the request server links against (batch launch, error text,
-// geometry), for compiling occastft_gb300/csrc/ocs_server.cpp without a GPU.
-// Geometry and option parsing are the library's own (ocs_host.cpp, linked
-// beside this file); only the device work is replaced.
+// TEST INFRASTRUCTURE ONLY: the host-only CUDA stand-in declared in
+// cuda_runtime.h.  Streams are FIFO worker threads, events record a
+// generation on the host and complete it in stream order, and
+// cudaStreamWaitEvent makes a stream's worker wait for that generation, so
+// work on different streams is ordered exactly as far as the events order
+// it.  An optional random delay before each unit of stream work shakes out
+// orderings that the events do not enforce.
 #include "cuda_runtime.h"
 #include "fake_control.h"
-#include "ocs_host.h"
-#include "ocs_internal.h"
 
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstdlib>
@@ -15,18 +16,47 @@
 #include <deque>
 #include <functional>
 #include <mutex>
+#include <random>
 #include <string>
 #include <thread>
+#include <utility>
 #include <vector>
 
 namespace fake {
 std::atomic<const void*> fail_copy_ptr{nullptr};
 std::atomic<int> stream_fail_after{-1};
+std::atomic<int> event_fail_after{-1};
+std::atomic<cudaStream_t> capturing{nullptr};
+std::atomic<int> jitter_us{0};
+std::atomic<int> h2d_delay_us{0};
 std::atomic<int> kernel_us{200};
 std::atomic<long> live_allocs{0};
+std::atomic<long> live_host_allocs{0};
 std::atomic<long> live_streams{0};
+std::atomic<long> live_events{0};
 std::atomic<long> launches{0};
 std::atomic<long> max_launch_requests{0};
+std::atomic<long> kernel_launches{0};
+
+namespace {
+std::mutex g_cap_mu;
+std::vector<std::pair<const void*, size_t>> g_captured;
+
+// creations left before a failure; false when this creation fails
+bool take(std::atomic<int>& left)
+{
+    int v = left.load();
+    while (v > 0 && !left.compare_exchange_weak(v, v - 1)) {
+    }
+    return v != 0;
+}
+}  // namespace
+
+void captured_sources(std::function<void(const void*, size_t)> fn)
+{
+    std::lock_guard<std::mutex> lk(g_cap_mu);
+    for (const auto& c : g_captured) fn(c.first, c.second);
+}
 }  // namespace fake
 
 // One stream: a worker thread running queued work in submission order.
@@ -50,6 +80,7 @@ struct FakeStream {
     }
     void run()
     {
+        std::mt19937 rng((unsigned)std::hash<std::thread::id>()(std::this_thread::get_id()));
         std::unique_lock<std::mutex> lk(mu);
         for (;;) {
             cv.wait(lk, [&] { return quit || !q.empty(); });
@@ -58,6 +89,8 @@ struct FakeStream {
             q.pop_front();
             busy = true;
             lk.unlock();
+            const int j = fake::jitter_us.load();
+            if (j > 0) std::this_thread::sleep_for(std::chrono::microseconds(rng() % (unsigned)(j + 1)));
             f();
             lk.lock();
             busy = false;
@@ -79,16 +112,36 @@ struct FakeStream {
     }
 };
 
+struct FakeEvent {
+    std::mutex mu;
+    std::condition_variable cv;
+    uint64_t recorded = 0, completed = 0;
+    double t_ms = 0.0;
+};
+
 namespace {
 thread_local cudaError_t t_last = cudaSuccess;
-thread_local std::string t_err;
 
 cudaError_t set_last(cudaError_t e)
 {
     t_last = e;
     return e;
 }
+
+// the legacy default stream (null handle)
+FakeStream* stream_of(cudaStream_t st)
+{
+    static FakeStream* legacy = new FakeStream();  // never destroyed
+    return st ? st : legacy;
+}
+
+double now_ms()
+{
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
 }  // namespace
+
+void fake::enqueue(cudaStream_t st, std::function<void()> fn) { stream_of(st)->push(std::move(fn)); }
 
 cudaError_t cudaGetDevice(int* device)
 {
@@ -96,6 +149,20 @@ cudaError_t cudaGetDevice(int* device)
     return cudaSuccess;
 }
 cudaError_t cudaSetDevice(int) { return cudaSuccess; }
+cudaError_t cudaGetDeviceProperties(cudaDeviceProp* p, int)
+{
+    std::memset(p, 0, sizeof(*p));
+    std::strcpy(p->name, "host stand-in");
+    p->major = 10;
+    p->minor = 3;
+    p->multiProcessorCount = 8;
+    return cudaSuccess;
+}
+cudaError_t cudaDeviceSynchronize(void)
+{
+    stream_of(nullptr)->sync();
+    return cudaSuccess;
+}
 cudaError_t cudaMemGetInfo(size_t* free_bytes, size_t* total_bytes)
 {
     *free_bytes = size_t(1) << 30;
@@ -104,7 +171,7 @@ cudaError_t cudaMemGetInfo(size_t* free_bytes, size_t* total_bytes)
 }
 cudaError_t cudaMalloc(void** p, size_t bytes)
 {
-    *p = std::aligned_alloc(256, (bytes + 255) & ~size_t(255));
+    *p = std::aligned_alloc(256, std::max<size_t>(256, (bytes + 255) & ~size_t(255)));
     if (!*p) return set_last(cudaErrorMemoryAllocation);
     ++fake::live_allocs;
     return cudaSuccess;
@@ -117,11 +184,39 @@ cudaError_t cudaFree(void* p)
     }
     return cudaSuccess;
 }
+cudaError_t cudaMallocAsync(void** p, size_t bytes, cudaStream_t) { return cudaMalloc(p, bytes); }
+cudaError_t cudaFreeAsync(void* p, cudaStream_t st)
+{
+    // freed once the stream's earlier work has run
+    stream_of(st)->push([p] { cudaFree(p); });
+    return cudaSuccess;
+}
+cudaError_t cudaHostAlloc(void** p, size_t bytes, unsigned)
+{
+    *p = std::aligned_alloc(256, std::max<size_t>(256, (bytes + 255) & ~size_t(255)));
+    if (!*p) return set_last(cudaErrorMemoryAllocation);
+    ++fake::live_host_allocs;
+    return cudaSuccess;
+}
+cudaError_t cudaFreeHost(void* p)
+{
+    if (p) {
+        std::free(p);
+        --fake::live_host_allocs;
+    }
+    return cudaSuccess;
+}
+cudaError_t cudaHostGetDevicePointer(void** d, void* h, unsigned)
+{
+    *d = h;
+    return cudaSuccess;
+}
+cudaError_t cudaHostRegister(void*, size_t, unsigned) { return cudaSuccess; }
+cudaError_t cudaHostUnregister(void*) { return cudaSuccess; }
+
 cudaError_t cudaStreamCreateWithFlags(cudaStream_t* st, unsigned)
 {
-    int left = fake::stream_fail_after.load();
-    if (left == 0) return set_last(cudaErrorMemoryAllocation);
-    if (left > 0) fake::stream_fail_after.store(left - 1);
+    if (!fake::take(fake::stream_fail_after)) return set_last(cudaErrorMemoryAllocation);
     *st = new FakeStream();
     ++fake::live_streams;
     return cudaSuccess;
@@ -129,26 +224,100 @@ cudaError_t cudaStreamCreateWithFlags(cudaStream_t* st, unsigned)
 cudaError_t cudaStreamDestroy(cudaStream_t st)
 {
     if (!st) return set_last(cudaErrorInvalidValue);
+    st->sync();
     delete st;
     --fake::live_streams;
     return cudaSuccess;
 }
 cudaError_t cudaStreamSynchronize(cudaStream_t st)
 {
-    if (!st) return set_last(cudaErrorInvalidValue);
-    st->sync();
+    stream_of(st)->sync();
     return cudaSuccess;
 }
-cudaError_t cudaMemcpyAsync(void* dst, const void* src, size_t bytes, cudaMemcpyKind, cudaStream_t st)
+cudaError_t cudaStreamIsCapturing(cudaStream_t st, cudaStreamCaptureStatus* status)
+{
+    *status = (st && st == fake::capturing.load()) ? cudaStreamCaptureStatusActive : cudaStreamCaptureStatusNone;
+    return cudaSuccess;
+}
+cudaError_t cudaEventCreateWithFlags(cudaEvent_t* ev, unsigned)
+{
+    if (!fake::take(fake::event_fail_after)) return set_last(cudaErrorMemoryAllocation);
+    *ev = new FakeEvent();
+    ++fake::live_events;
+    return cudaSuccess;
+}
+cudaError_t cudaEventCreate(cudaEvent_t* ev) { return cudaEventCreateWithFlags(ev, 0); }
+cudaError_t cudaEventDestroy(cudaEvent_t ev)
+{
+    if (!ev) return set_last(cudaErrorInvalidValue);
+    { std::lock_guard<std::mutex> lk(ev->mu); }  // a completing record has left it
+    delete ev;
+    --fake::live_events;
+    return cudaSuccess;
+}
+cudaError_t cudaEventRecord(cudaEvent_t ev, cudaStream_t st)
+{
+    uint64_t gen;
+    {
+        std::lock_guard<std::mutex> lk(ev->mu);
+        gen = ++ev->recorded;
+    }
+    stream_of(st)->push([ev, gen] {
+        // signalled under the lock: a host thread that sees the completion
+        // may destroy the event at once, as it may a CUDA event
+        std::lock_guard<std::mutex> lk(ev->mu);
+        ev->completed = std::max(ev->completed, gen);
+        ev->t_ms = now_ms();
+        ev->cv.notify_all();
+    });
+    return cudaSuccess;
+}
+cudaError_t cudaStreamWaitEvent(cudaStream_t st, cudaEvent_t ev, unsigned)
+{
+    uint64_t gen;
+    {
+        std::lock_guard<std::mutex> lk(ev->mu);
+        gen = ev->recorded;
+    }
+    if (gen == 0) return cudaSuccess;  // never recorded: nothing to wait for
+    stream_of(st)->push([ev, gen] {
+        std::unique_lock<std::mutex> lk(ev->mu);
+        ev->cv.wait(lk, [&] { return ev->completed >= gen; });
+    });
+    return cudaSuccess;
+}
+cudaError_t cudaEventSynchronize(cudaEvent_t ev)
+{
+    std::unique_lock<std::mutex> lk(ev->mu);
+    const uint64_t gen = ev->recorded;
+    ev->cv.wait(lk, [&] { return ev->completed >= gen; });
+    return cudaSuccess;
+}
+cudaError_t cudaEventElapsedTime(float* ms, cudaEvent_t start, cudaEvent_t end)
+{
+    std::lock_guard<std::mutex> a(start->mu);
+    std::lock_guard<std::mutex> b(end->mu);
+    *ms = (float)std::max(0.0, end->t_ms - start->t_ms);
+    return cudaSuccess;
+}
+cudaError_t cudaMemcpyAsync(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t st)
 {
     const void* bad = fake::fail_copy_ptr.load();
     if (bad && (bad == src || bad == dst)) return set_last(cudaErrorInvalidValue);
-    st->push([=] { std::memcpy(dst, src, bytes); });
+    if (st && st == fake::capturing.load() && kind == cudaMemcpyHostToDevice) {
+        std::lock_guard<std::mutex> lk(fake::g_cap_mu);
+        fake::g_captured.emplace_back(src, bytes);
+    }
+    const int delay = kind == cudaMemcpyHostToDevice ? fake::h2d_delay_us.load() : 0;
+    stream_of(st)->push([=] {
+        if (delay > 0) std::this_thread::sleep_for(std::chrono::microseconds(delay));
+        std::memcpy(dst, src, bytes);
+    });
     return cudaSuccess;
 }
 cudaError_t cudaLaunchHostFunc(cudaStream_t st, cudaHostFn_t fn, void* arg)
 {
-    st->push([=] { fn(arg); });
+    stream_of(st)->push([=] { fn(arg); });
     return cudaSuccess;
 }
 cudaError_t cudaGetLastError(void)
@@ -157,79 +326,4 @@ cudaError_t cudaGetLastError(void)
     t_last = cudaSuccess;
     return e;
 }
-const char* cudaGetErrorString(cudaError_t e) { return e ? "fake CUDA error" : "no error"; }
-
-namespace ocs {
-void set_last_error(const std::string& msg) { t_err = msg; }
-
-namespace internal {
-
-// The batch launch: validates each request as the library does and queues one
-// unit of stream work that writes fake::expected() into every output.
-int batch_enqueue(ocs_request* reqs, int count, cudaStream_t st, BatchScratch&)
-{
-    struct Item {
-        const float* in;
-        uint64_t n;
-        int exp;
-        float* out;
-        uint64_t out_floats;
-    };
-    std::vector<Item> items;
-    for (int i = 0; i < count; ++i) {
-        ocs_request& q = reqs[i];
-        Options o;
-        Geometry g;
-        std::string st_msg = parse_options(q.options, o);
-        q.status = st_msg == "OK" ? OCS_OK : OCS_EPIPELINE;
-        if (q.status == OCS_OK && make_geometry(q.n, q.window_size_exp, q.overlap_ratio, o, g) != "OK")
-            q.status = OCS_EINVAL;
-        if (q.status == OCS_OK && q.out_cap < g.out_floats) q.status = OCS_ESPACE;
-        if (q.status == OCS_OK) items.push_back(Item{q.in, q.n, q.window_size_exp, q.out, g.out_floats});
-    }
-    ++fake::launches;
-    long prev = fake::max_launch_requests.load();
-    while (prev < count && !fake::max_launch_requests.compare_exchange_weak(prev, count)) {
-    }
-    const int us = fake::kernel_us.load();
-    st->push([items, us] {
-        std::this_thread::sleep_for(std::chrono::microseconds(us));
-        for (const Item& it : items)
-            for (uint64_t k = 0; k < it.out_floats; ++k) it.out[k] = fake::expected(it.in, it.n, it.exp, k);
-    });
-    return OCS_OK;
-}
-
-void batch_scratch_release(BatchScratch& b) { b = BatchScratch{}; }
-int ensure_ready() { return OCS_OK; }
-void set_error(int, const std::string& msg) { t_err = msg; }
-
-}  // namespace internal
-}  // namespace ocs
-
-extern "C" int ocs_geometry_get(uint64_t n, int exp, float ov, const char* options, ocs_geometry* out)
-{
-    ocs::Options o;
-    ocs::Geometry g;
-    std::string s = ocs::parse_options(options, o);
-    if (s != "OK") {
-        t_err = s;
-        return OCS_EPIPELINE;
-    }
-    s = ocs::make_geometry(n, exp, ov, o, g);
-    if (s != "OK") {
-        t_err = s;
-        return OCS_EINVAL;
-    }
-    std::memset(out, 0, sizeof(*out));
-    out->qt = g.qt;
-    out->hop = g.hop;
-    out->ofull = g.ofull;
-    out->ohalf = g.ohalf;
-    out->n_window = g.n_window;
-    out->out_floats = g.out_floats;
-    out->frames = g.frames;
-    return OCS_OK;
-}
-
-extern "C" const char* ocs_last_error(void) { return t_err.c_str(); }
+const char* cudaGetErrorString(cudaError_t e) { return e ? "stand-in CUDA error" : "no error"; }

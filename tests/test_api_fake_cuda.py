@@ -1,0 +1,63 @@
+"""The C ABI's host logic on the CPU: occastft_gb300/csrc/ocs_api.cpp compiled
+unchanged against a host-only CUDA stand-in (tests/fake_cuda/) whose streams
+are FIFO worker threads ordered by events as CUDA's are, and whose stand-in
+kernels read each frame's samples and write the floats the layout gives that
+frame.  Built with ThreadSanitizer where the compiler has it.
+
+Covers what the GPU tests cannot make happen on purpose or often enough:
+- a request slot or a kernel-variant timing whose streams or events cannot be
+  created (nothing may leak);
+- the chunked copy/compute pipeline of ocs_activate under random delays on
+  every stream and slow input copies, with the result written over the
+  signal in three placements;
+- four threads calling ocs_activate at once;
+- uneven batches, the per-capture descriptor buffers, and a full release at
+  ocs_shutdown."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+FAKE = os.path.join(ROOT, "tests", "fake_cuda")
+CSRC = os.path.join(ROOT, "occastft_gb300", "csrc")
+SOURCES = [os.path.join(CSRC, "ocs_api.cpp"), os.path.join(CSRC, "ocs_host.cpp"),
+           os.path.join(FAKE, "fake_runtime.cpp"), os.path.join(FAKE, "fake_kernels.cpp"),
+           os.path.join(FAKE, "api_stress.cpp")]
+CHECKS = ["slot_fail", "tune_fail", "activate", "concurrent", "batch", "capture", "shutdown"]
+
+
+def _build(out, sanitize):
+    cxx = os.environ.get("CXX", "g++")
+    cmd = [cxx, "-std=c++17", "-O1", "-g", "-pthread", "-I" + FAKE, "-I" + CSRC] + sanitize + SOURCES + ["-o", out]
+    return subprocess.run(cmd, capture_output=True, text=True, timeout=300)
+
+
+@pytest.fixture(scope="module")
+def run(tmp_path_factory):
+    if not shutil.which(os.environ.get("CXX", "g++")):
+        pytest.skip("no C++ compiler")
+    out = str(tmp_path_factory.mktemp("api_stress") / "api_stress")
+    r = _build(out, ["-fsanitize=thread"])
+    tsan = r.returncode == 0
+    if not tsan:
+        r = _build(out, [])
+    assert r.returncode == 0, r.stderr[-4000:]
+    env = dict(os.environ, TSAN_OPTIONS="halt_on_error=1 exitcode=66")
+    env.pop("OCS_TUNE_CACHE", None)
+    p = subprocess.run([out], capture_output=True, text=True, timeout=900, env=env)
+    return p, tsan
+
+
+@pytest.mark.parametrize("check", CHECKS)
+def test_c_abi_host_logic(run, check):
+    p, tsan = run
+    assert f"ok {check}" in p.stdout, (p.stdout + p.stderr)[-4000:]
+    if tsan:
+        assert "ThreadSanitizer" not in p.stderr, p.stderr[-4000:]
+
+
+def test_c_abi_host_logic_exit(run):
+    p, _ = run
+    assert p.returncode == 0 and "all ok" in p.stdout, (p.stdout + p.stderr)[-4000:]

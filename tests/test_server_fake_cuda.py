@@ -18,7 +18,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 FAKE = os.path.join(ROOT, "tests", "fake_cuda")
 CSRC = os.path.join(ROOT, "occastft_gb300", "csrc")
 SOURCES = [os.path.join(CSRC, "ocs_server.cpp"), os.path.join(CSRC, "ocs_host.cpp"),
-           os.path.join(FAKE, "fake_runtime.cpp"), os.path.join(FAKE, "server_stress.cpp")]
+           os.path.join(FAKE, "fake_runtime.cpp"), os.path.join(FAKE, "fake_server_internal.cpp"),
+           os.path.join(FAKE, "server_stress.cpp")]
 
 
 def _build(out, sanitize):
