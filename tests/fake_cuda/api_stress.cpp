@@ -22,6 +22,7 @@
 //   shutdown      ocs_shutdown releases every allocation, stream and event
 #include "../../include/occastft_gb300.h"
 #include "fake_control.h"
+#include "fake_expect.h"
 
 #include <cmath>
 #include <cstdio>
@@ -42,37 +43,14 @@ void check(bool ok, const char* name, const std::string& why)
     std::exit(1);
 }
 
-bool has(const std::string& s, const char* o) { return s.find(o) != std::string::npos; }
-
-// the result the stand-in kernels produce for a whole request
 std::vector<float> expected_out(const float* x, uint64_t n, int exp, float ov, const std::string& opts)
 {
-    ocs_geometry g;
-    check(ocs_geometry_get(n, exp, ov, opts.c_str(), &g) == OCS_OK, "expected_out", "geometry");
-    const uint64_t N = 1ull << exp;
-    const bool half = has(opts, "--half_complex_return"), dense = has(opts, "--layout=dense");
-    const uint64_t row = dense ? (N / 2 + 1) * (half ? 2 : 1) : (half ? 2 * N : N);
-    std::vector<float> out(g.out_floats, std::nanf(""));
-    for (uint64_t f = 0; f < g.frames; ++f)
-        for (uint64_t k = 0; k < row; ++k) {
-            const uint64_t idx = f * row + k;
-            if (idx >= g.out_floats) break;
-            const uint64_t s = f * g.hop + k % N;
-            out[idx] = s < n ? x[s] : 0.0f;
-        }
-    return out;
+    std::vector<float> v = fake::expected_out(x, n, exp, ov, opts);
+    check(!v.empty(), "expected_out", "geometry");
+    return v;
 }
 
-std::vector<float> make_signal(uint64_t n, uint32_t seed)
-{
-    std::vector<float> x(n);
-    uint32_t v = seed * 2654435761u + 1;
-    for (auto& s : x) {
-        v = v * 1664525u + 1013904223u;
-        s = (float)(v >> 8) * (1.0f / 16777216.0f) + 1.0f;  // never 0: zero padding stays visible
-    }
-    return x;
-}
+using fake::make_signal;
 
 const char* kOpts[] = {"--hanning_window", "--hamming_window --half_complex_return", "--blackman_window --layout=dense",
                        "--hanning_window --half_complex_return --layout=dense", "--remove_dc --serial_power"};
