@@ -103,7 +103,7 @@ void activate()
     std::mt19937_64 rng(12345);
     const int exps[] = {6, 7, 8, 9, 10, 12, 13, 16};
     const float ovs[] = {0.0f, 0.25f, 0.5f, 0.75f, 0.3f};
-    int cases = 0, multi = 0;
+    int cases = 0, multi = 0, large_small_budget = 0;
     for (int c = 0; c < 40; ++c) {
         const int exp = exps[rng() % 8];
         const float ov = ovs[rng() % 5];
@@ -135,8 +135,13 @@ void activate()
         // every other request with slow input copies: a result copy that did
         // not wait for the input it overwrites would then overtake it
         fake::h2d_delay_us = (c / 4) % 2 ? 4000 : 0;
+        // windows above 2^15 run in launch pairs over frame ranges sized by a
+        // scratch budget: a 1 MB budget makes many of them per chunk
+        const bool small_budget = c % 3 != 2;
+        if (small_budget) setenv("OCS_LARGE_SCRATCH_MB", "1", 1);
         uint64_t len = 0;
         const int rc = ocs_activate(in, n, exp, ov, opts.c_str(), out, g.out_floats, &len);
+        unsetenv("OCS_LARGE_SCRATCH_MB");
         fake::h2d_delay_us = 0;
         const std::string tag = "case " + std::to_string(c) + " exp " + std::to_string(exp) + " ov " +
                                 std::to_string(ov) + " n " + std::to_string(n) + " alias " + std::to_string(alias) +
@@ -145,10 +150,12 @@ void activate()
         check(std::memcmp(out, want.data(), g.out_floats * 4) == 0, name, tag + ": result differs");
         ++cases;
         multi += n > 2200000;
+        large_small_budget += exp >= 16 && small_budget;
     }
     fake::jitter_us = 0;
-    check(cases >= 30 && multi >= 15, name, "too few cases ran");
-    std::printf("ok %s (%d requests, %d with several chunks)\n", name, cases, multi);
+    check(cases >= 30 && multi >= 15 && large_small_budget >= 2, name, "too few cases ran");
+    std::printf("ok %s (%d requests, %d with several chunks, %d large windows on a 1 MB scratch budget)\n", name,
+                cases, multi, large_small_budget);
 }
 
 void concurrent()
