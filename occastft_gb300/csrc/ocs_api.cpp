@@ -397,7 +397,8 @@ int launch_large_frames(const Request& r, const float* d_sig, uint64_t n, float*
     // at 1e8 samples: chunks small enough for the scratch to stay in L2
     // (16-96 MB) lose to fewer, fuller launch pairs; 1 GB is the default
     uint64_t scratch_bytes = 1024ull << 20;
-    if (const char* sb = std::getenv("OCS_LARGE_SCRATCH_MB")) scratch_bytes = std::max(1L, std::atol(sb)) << 20;
+    if (const char* sb = std::getenv("OCS_LARGE_SCRATCH_MB"))
+        scratch_bytes = (uint64_t)std::min(std::max(1L, std::atol(sb)), 1L << 20) << 20;  // 1 MB .. 1 TB
     const uint64_t per = std::max<uint64_t>(1, std::min<uint64_t>(f1 - f0, scratch_bytes / (M * sizeof(float2))));
     float2* scratch = nullptr;
     OCS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&scratch), per * M * sizeof(float2), st));
