@@ -112,10 +112,20 @@ int init_locked(Context& c, int device)
     c.device = device;
     c.sms = p.multiProcessorCount;
     c.gpu_name = p.name;
-    OCS_CUDA(cudaStreamCreateWithFlags(&c.s_setup, cudaStreamNonBlocking));
-    OCS_CUDA(cudaHostAlloc(&c.h_err, sizeof(int), cudaHostAllocMapped));
-    *reinterpret_cast<volatile int*>(c.h_err) = 0;
-    OCS_CUDA(cudaHostGetDevicePointer(&c.d_err, c.h_err, 0));
+    cudaError_t e = cudaStreamCreateWithFlags(&c.s_setup, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaHostAlloc(&c.h_err, sizeof(int), cudaHostAllocMapped);
+    if (e == cudaSuccess) {
+        *reinterpret_cast<volatile int*>(c.h_err) = 0;
+        e = cudaHostGetDevicePointer(&c.d_err, c.h_err, 0);
+    }
+    if (e != cudaSuccess) {  // a later call starts over from nothing
+        if (c.h_err) cudaFreeHost(c.h_err);
+        if (c.s_setup) cudaStreamDestroy(c.s_setup);
+        c.h_err = nullptr;
+        c.d_err = nullptr;
+        c.s_setup = nullptr;
+        return cuda_fail(e, "runner set-up");
+    }
     const char* stall = std::getenv("OCS_TC_TEST_STALL");
     c.tc_test_stall = (stall && stall[0] == '1') ? 1 : 0;
     c.ready = true;
@@ -155,8 +165,12 @@ int get_twiddles(int exp, bool paired, const float2** out)
     float2* d = nullptr;
     const int n = paired ? ocs::pair_twiddle_count(exp) : ocs::fused_twiddle_count(exp);
     OCS_CUDA(cudaMalloc(&d, sizeof(float2) * n));
-    OCS_CUDA(paired ? ocs::build_pair_twiddles(d, exp, c.s_setup) : ocs::build_twiddles(d, exp, c.s_setup));
-    OCS_CUDA(cudaStreamSynchronize(c.s_setup));
+    cudaError_t e = paired ? ocs::build_pair_twiddles(d, exp, c.s_setup) : ocs::build_twiddles(d, exp, c.s_setup);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.s_setup);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return cuda_fail(e, "twiddle table");
+    }
     c.twiddles[key] = d;
     *out = d;
     return OCS_OK;
@@ -184,8 +198,12 @@ int get_window(int kind, int exp, float sigma, bool scaled, const float** out)
         for (float& v : w) v *= 0.5f;
     float* d = nullptr;
     OCS_CUDA(cudaMalloc(&d, sizeof(float) * w.size()));
-    OCS_CUDA(cudaMemcpyAsync(d, w.data(), sizeof(float) * w.size(), cudaMemcpyHostToDevice, c.s_setup));
-    OCS_CUDA(cudaStreamSynchronize(c.s_setup));
+    cudaError_t e = cudaMemcpyAsync(d, w.data(), sizeof(float) * w.size(), cudaMemcpyHostToDevice, c.s_setup);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c.s_setup);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return cuda_fail(e, "window table");
+    }
     c.windows[key] = d;
     if (exp <= 8) c.windows_host[d] = w;  // the lanes-per-frame kernels take it as a parameter
     *out = d;
@@ -358,8 +376,12 @@ int get_two_level(uint64_t L, const float2** lo, const float2** hi)
         float2* d = nullptr;
         const uint64_t nhi = (L + 1023) / 1024;
         OCS_CUDA(cudaMalloc(&d, sizeof(float2) * (1024 + nhi)));
-        OCS_CUDA(ocs::build_two_level(d, d + 1024, L, c.s_setup));
-        OCS_CUDA(cudaStreamSynchronize(c.s_setup));
+        cudaError_t e = ocs::build_two_level(d, d + 1024, L, c.s_setup);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c.s_setup);
+        if (e != cudaSuccess) {
+            cudaFree(d);
+            return cuda_fail(e, "two-level twiddle table");
+        }
         it = c.two_level.emplace(L, d).first;
     }
     *lo = it->second;

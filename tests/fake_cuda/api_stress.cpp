@@ -3,6 +3,9 @@
 // CUDA stand-in and stand-in kernels in this folder.  Each check prints
 // "ok <name>"; the first failure prints "FAIL <name>: <why>" and exits 1.
 //
+//   setup_fail    a set-up whose pinned error word cannot be allocated
+//                 releases its stream, and a later ocs_init starts over
+//   table_fail    a window table whose upload cannot be issued is freed
 //   slot_fail     a request slot whose streams cannot all be created is
 //                 released again (no stream or event left behind)
 //   tune_fail     a kernel-variant timing whose events cannot be created
@@ -54,6 +57,50 @@ using fake::make_signal;
 
 const char* kOpts[] = {"--hanning_window", "--hamming_window --half_complex_return", "--blackman_window --layout=dense",
                        "--hanning_window --half_complex_return --layout=dense", "--remove_dc --serial_power"};
+
+void setup_fail()
+{
+    const char* name = "setup_fail";
+    fake::host_alloc_fail_after = 0;
+    const int rc = ocs_init(0);
+    fake::host_alloc_fail_after = -1;
+    check(rc == OCS_ECUDA, name, "rc " + std::to_string(rc));
+    check(fake::live_streams.load() == 0 && fake::live_host_allocs.load() == 0, name, "set-up objects left behind");
+    check(ocs_init(0) == OCS_OK, name, "a second ocs_init");
+    check(fake::live_streams.load() == 1 && fake::live_host_allocs.load() == 1, name, "set-up objects");
+    std::printf("ok %s\n", name);
+}
+
+void table_fail()
+{
+    const char* name = "table_fail";
+    // the device entry point makes no input copies: the first host-to-device
+    // copy is the new window table's upload
+    std::vector<float> x = make_signal(20000, 3);
+    float* d_in = nullptr;
+    float* d_out = nullptr;
+    ocs_geometry g;
+    const char* opts = "--blackman_harris_window";
+    check(ocs_geometry_get(x.size(), 7, 0.5f, opts, &g) == OCS_OK, name, "geometry");
+    check(cudaMalloc(&d_in, x.size() * 4) == cudaSuccess && cudaMalloc(&d_out, g.out_floats * 4) == cudaSuccess, name,
+          "alloc");
+    std::memcpy(d_in, x.data(), x.size() * 4);
+    const long allocs0 = fake::live_allocs.load();
+    fake::h2d_fail_after = 0;
+    const int rc = ocs_activate_device(d_in, x.size(), 7, 0.5f, opts, d_out, g.out_floats, nullptr);
+    fake::h2d_fail_after = -1;
+    check(rc == OCS_ECUDA, name, "rc " + std::to_string(rc));
+    // the twiddle tables of window 2^7 stay (they were built); the window table must not
+    const long allocs1 = fake::live_allocs.load();
+    check(allocs1 - allocs0 == 2, name, "allocations after the failed upload: " + std::to_string(allocs1 - allocs0));
+    check(ocs_activate_device(d_in, x.size(), 7, 0.5f, opts, d_out, g.out_floats, nullptr) == OCS_OK, name, "retry");
+    cudaStreamSynchronize(nullptr);
+    check(std::memcmp(d_out, expected_out(x.data(), x.size(), 7, 0.5f, opts).data(), g.out_floats * 4) == 0, name,
+          "result after the retry");
+    cudaFree(d_in);
+    cudaFree(d_out);
+    std::printf("ok %s\n", name);
+}
 
 void slot_fail()
 {
@@ -336,7 +383,8 @@ void shutdown()
 int main()
 {
     setenv("OCS_AUTOTUNE", "0", 1);
-    check(ocs_init(0) == OCS_OK, "init", "ocs_init");
+    setup_fail();
+    table_fail();
     slot_fail();
     tune_fail();
     activate();

@@ -14,6 +14,9 @@ extern std::atomic<const void*> fail_copy_ptr;
 // creations left before cudaStreamCreateWithFlags / cudaEventCreate* fail (< 0: never)
 extern std::atomic<int> stream_fail_after;
 extern std::atomic<int> event_fail_after;
+// likewise for cudaHostAlloc and for host-to-device copies
+extern std::atomic<int> host_alloc_fail_after;
+extern std::atomic<int> h2d_fail_after;
 // the stream cudaStreamIsCapturing reports as capturing (null: none)
 extern std::atomic<cudaStream_t> capturing;
 // source addresses of the host-to-device copies issued on `capturing`

@@ -26,6 +26,8 @@ namespace fake {
 std::atomic<const void*> fail_copy_ptr{nullptr};
 std::atomic<int> stream_fail_after{-1};
 std::atomic<int> event_fail_after{-1};
+std::atomic<int> host_alloc_fail_after{-1};
+std::atomic<int> h2d_fail_after{-1};
 std::atomic<cudaStream_t> capturing{nullptr};
 std::atomic<int> jitter_us{0};
 std::atomic<int> h2d_delay_us{0};
@@ -193,6 +195,7 @@ cudaError_t cudaFreeAsync(void* p, cudaStream_t st)
 }
 cudaError_t cudaHostAlloc(void** p, size_t bytes, unsigned)
 {
+    if (!fake::take(fake::host_alloc_fail_after)) return set_last(cudaErrorMemoryAllocation);
     *p = std::aligned_alloc(256, std::max<size_t>(256, (bytes + 255) & ~size_t(255)));
     if (!*p) return set_last(cudaErrorMemoryAllocation);
     ++fake::live_host_allocs;
@@ -304,6 +307,7 @@ cudaError_t cudaMemcpyAsync(void* dst, const void* src, size_t bytes, cudaMemcpy
 {
     const void* bad = fake::fail_copy_ptr.load();
     if (bad && (bad == src || bad == dst)) return set_last(cudaErrorInvalidValue);
+    if (kind == cudaMemcpyHostToDevice && !fake::take(fake::h2d_fail_after)) return set_last(cudaErrorInvalidValue);
     if (st && st == fake::capturing.load() && kind == cudaMemcpyHostToDevice) {
         std::lock_guard<std::mutex> lk(fake::g_cap_mu);
         fake::g_captured.emplace_back(src, bytes);

@@ -5,8 +5,8 @@ kernels read each frame's samples and write the floats the layout gives that
 frame.  Built with ThreadSanitizer where the compiler has it.
 
 Covers what the GPU tests cannot make happen on purpose or often enough:
-- a request slot or a kernel-variant timing whose streams or events cannot be
-  created (nothing may leak);
+- a set-up, a window table upload, a request slot or a kernel-variant timing
+  whose allocation, copy, streams or events fail (nothing may leak);
 - the chunked copy/compute pipeline of ocs_activate under random delays on
   every stream and slow input copies, with the result written over the
   signal in three placements;
@@ -25,7 +25,7 @@ CSRC = os.path.join(ROOT, "occastft_gb300", "csrc")
 SOURCES = [os.path.join(CSRC, "ocs_api.cpp"), os.path.join(CSRC, "ocs_host.cpp"),
            os.path.join(FAKE, "fake_runtime.cpp"), os.path.join(FAKE, "fake_kernels.cpp"),
            os.path.join(FAKE, "api_stress.cpp")]
-CHECKS = ["slot_fail", "tune_fail", "activate", "concurrent", "batch", "capture", "shutdown"]
+CHECKS = ["setup_fail", "table_fail", "slot_fail", "tune_fail", "activate", "concurrent", "batch", "capture", "shutdown"]
 
 
 def _build(out, sanitize):
