@@ -198,3 +198,19 @@ def test_proxy_drives_the_runner(stand_in_runner, ocs_lib, tmp_path):
             assert got is not None and np.array_equal(got[: want.size], want), (exp, ov, opts)
     finally:
         assert p.kill_runner()
+
+
+def test_proxy_remote_server(served, ocs_lib):
+    """A "SERVER" runtime: the proxy connects to a runner that is already
+    listening and sends the signal in the data list instead of shared memory
+    (STFTProxy.cpp:118-154, FFTStruct.cpp data-list path)."""
+    p = proxy.STFTProxy([("SERVER", f"127.0.0.1:{served}")])
+    try:
+        assert p.status == "OK" and p.gpu_type == "SERVER"
+        for exp, ov, opts in CASES[:4]:
+            x = signal(exp + 90, 98_765)
+            got = p.request_stft(x, exp, ov, opts)
+            want = stand_in_out(ocs_lib, x, exp, ov, opts)
+            assert got is not None and np.array_equal(got, want), (exp, ov, opts)
+    finally:
+        p.ws.close()  # the shared runner keeps serving the other tests
