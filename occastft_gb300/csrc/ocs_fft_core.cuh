@@ -26,7 +26,9 @@ struct FusedCfg {
 };
 
 // Values per thread by window exponent (index 6..15); 32 values per thread
-// give one shared-memory exchange up to 2^11 at the cost of registers.
+// give one shared-memory exchange up to 2^11 at the cost of registers.  The
+// table is the measured choice; -DOCS_R_TABLE={...} builds a variant library
+// for sweeps of the plan (loaded through OCS_LIBRARY).
 #ifndef OCS_R_TABLE
 #define OCS_R_TABLE {16, 8, 16, 16, 16, 32, 16, 16, 16, 32}
 #endif
