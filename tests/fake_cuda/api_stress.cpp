@@ -23,6 +23,11 @@
 //                 batch does not touch them; a capture without a preceding
 //                 ocs_batch_prepare is refused
 //   shutdown      ocs_shutdown releases every allocation, stream and event
+//
+// With arguments it runs one half of the tuning-cache check instead, each in
+// a fresh process: "tune-cache-write <file>" tunes one request with
+// OCS_TUNE_CACHE=<file>; "tune-cache-read <file>" runs the same request where
+// no event can be created, so it succeeds only on the cached choice.
 #include "../../include/occastft_gb300.h"
 #include "fake_control.h"
 #include "fake_expect.h"
@@ -380,8 +385,45 @@ void shutdown()
 
 }  // namespace
 
-int main()
+// one request whose window and size class need a kernel-variant choice
+int tune_cache_request()
 {
+    std::vector<float> x = make_signal(300000, 42);
+    ocs_geometry g;
+    if (ocs_geometry_get(x.size(), 10, 0.5f, "--hamming_window", &g) != OCS_OK) return OCS_EINVAL;
+    std::vector<float> out(g.out_floats);
+    uint64_t len = 0;
+    const int rc = ocs_activate(x.data(), x.size(), 10, 0.5f, "--hamming_window", out.data(), out.size(), &len);
+    if (rc == OCS_OK &&
+        std::memcmp(out.data(), expected_out(x.data(), x.size(), 10, 0.5f, "--hamming_window").data(),
+                    out.size() * 4) != 0)
+        return -1;
+    return rc;
+}
+
+int tune_cache(const std::string& mode, const char* file)
+{
+    setenv("OCS_AUTOTUNE", "1", 1);
+    setenv("OCS_TUNE_CACHE", file, 1);
+    check(ocs_init(0) == OCS_OK, "tune_cache", "ocs_init");
+    if (mode == "tune-cache-read") {
+        // the slot's own events first; after that no event can be created
+        std::vector<float> x = make_signal(100, 1), out(1 << 12);
+        uint64_t len = 0;
+        check(ocs_activate(x.data(), x.size(), 6, 0.5f, "", out.data(), out.size(), &len) == OCS_OK, "tune_cache",
+              "warm");
+        fake::event_fail_after = 0;
+    }
+    const int rc = tune_cache_request();
+    check(rc == OCS_OK, "tune_cache", mode + ": rc " + std::to_string(rc));
+    ocs_shutdown();
+    std::printf("ok %s\n", mode.c_str());
+    return 0;
+}
+
+int main(int argc, char** argv)
+{
+    if (argc == 3) return tune_cache(argv[1], argv[2]);
     setenv("OCS_AUTOTUNE", "0", 1);
     setup_fail();
     table_fail();

@@ -35,7 +35,7 @@ def _build(out, sanitize):
 
 
 @pytest.fixture(scope="module")
-def run(tmp_path_factory):
+def api_bin(tmp_path_factory):
     if not shutil.which(os.environ.get("CXX", "g++")):
         pytest.skip("no C++ compiler")
     out = str(tmp_path_factory.mktemp("api_stress") / "api_stress")
@@ -44,9 +44,19 @@ def run(tmp_path_factory):
     if not tsan:
         r = _build(out, [])
     assert r.returncode == 0, r.stderr[-4000:]
+    return out, tsan
+
+
+def _env():
     env = dict(os.environ, TSAN_OPTIONS="halt_on_error=1 exitcode=66")
     env.pop("OCS_TUNE_CACHE", None)
-    p = subprocess.run([out], capture_output=True, text=True, timeout=900, env=env)
+    return env
+
+
+@pytest.fixture(scope="module")
+def run(api_bin):
+    exe, tsan = api_bin
+    p = subprocess.run([exe], capture_output=True, text=True, timeout=900, env=_env())
     return p, tsan
 
 
@@ -61,3 +71,25 @@ def test_c_abi_host_logic(run, check):
 def test_c_abi_host_logic_exit(run):
     p, _ = run
     assert p.returncode == 0 and "all ok" in p.stdout, (p.stdout + p.stderr)[-4000:]
+
+
+def test_tuning_cache_round_trip(api_bin, tmp_path):
+    """OCS_TUNE_CACHE: one process tunes a request and appends its choice
+    ("gpu|exp|outk|dense|bucket|variant"); a second process, in which no
+    event can be created, runs the same request on the cached choice alone.
+    Lines for other GPUs and malformed lines are skipped."""
+    exe, _ = api_bin
+    cache = tmp_path / "tune.txt"
+    cache.write_text("not a cache line\nanother gpu|10|0|0|9|1\n")
+    w = subprocess.run([exe, "tune-cache-write", str(cache)], capture_output=True, text=True, timeout=300, env=_env())
+    assert w.returncode == 0 and "ok tune-cache-write" in w.stdout, w.stdout + w.stderr
+    lines = cache.read_text().splitlines()
+    assert lines[:2] == ["not a cache line", "another gpu|10|0|0|9|1"]
+    mine = [ln.split("|") for ln in lines[2:]]
+    assert mine and all(len(f) == 6 and f[0] == "host stand-in" for f in mine), lines
+    r = subprocess.run([exe, "tune-cache-read", str(cache)], capture_output=True, text=True, timeout=300, env=_env())
+    assert r.returncode == 0 and "ok tune-cache-read" in r.stdout, r.stdout + r.stderr
+    # without the cached line the same run has to time the variants, and cannot
+    cache.write_text("not a cache line\n")
+    r = subprocess.run([exe, "tune-cache-read", str(cache)], capture_output=True, text=True, timeout=300, env=_env())
+    assert r.returncode != 0 and "kernel variant timing" in r.stdout
