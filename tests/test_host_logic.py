@@ -171,3 +171,53 @@ def test_activate_out_argument_is_checked(ocs_lib):
     ro.flags.writeable = False
     with pytest.raises(ocs_lib.OcsError, match="float32 numpy array"):
         ocs_lib.activate(x, 6, 0.5, "", out=ro)
+
+
+def test_validation_before_any_device_call(ocs_lib):
+    """Arguments the C ABI refuses before it touches a device, with the
+    reference's status strings where it has one: these run on a machine
+    without a GPU.  Addresses are plain integers that are never dereferenced."""
+    L = ocs_lib.lib()
+    P = 0x10000
+
+    def err(rc, code, text):
+        assert rc == code, (rc, ocs_lib.last_error())
+        assert text in ocs_lib.last_error(), ocs_lib.last_error()
+
+    # per-stage hooks (runnerFunction::*)
+    err(L.ocs_stage_fft(P, P, 1024, 5, None), ocs_lib.OCS_EINVAL, "Operation not supported")
+    err(L.ocs_stage_fft(P, P, 1024, 16, None), ocs_lib.OCS_EINVAL, "above 2^15")
+    err(L.ocs_stage_fft(None, P, 1024, 10, None), ocs_lib.OCS_EINVAL, "null buffer")
+    err(L.ocs_stage_window(0, P, 1024, 1024, -1.0, None), ocs_lib.OCS_EINVAL, "window")
+    err(L.ocs_stage_window(1, P, 1024, 1000, -1.0, None), ocs_lib.OCS_EINVAL, "window")
+    err(L.ocs_stage_window(1, P, 1 << 17, 1 << 16, -1.0, None), ocs_lib.OCS_EINVAL, "above 2^15")
+    err(L.ocs_stage_remove_dc(None, 1, 1024, 1024, None), ocs_lib.OCS_EINVAL, "RemoveDC")
+    err(L.ocs_stage_overlap(P, 1024, 1000, 5, 512, P, None), ocs_lib.OCS_EINVAL, "Overlap")
+    err(L.ocs_stage_half_complex(None, P, P, 512, 10, None), ocs_lib.OCS_EINVAL, "HalfComplex")
+    err(L.ocs_stage_to_power(P, None, P, 1024, None), ocs_lib.OCS_EINVAL, "ToPower")
+    # whole-pipeline entry points
+    g = ocs_lib.geometry(100000, 10, 0.5, "")
+    n_out = ctypes.c_uint64()
+    err(L.ocs_activate(P, 100000, 10, 0.5, b"", P, g.out_floats - 1, ctypes.byref(n_out)), ocs_lib.OCS_ESPACE,
+        "too small")
+    err(L.ocs_activate(None, 100000, 10, 0.5, b"", P, g.out_floats, ctypes.byref(n_out)), ocs_lib.OCS_EINVAL, "null")
+    err(L.ocs_activate_device(P, 100000, 10, 0.5, b"", None, g.out_floats, None), ocs_lib.OCS_EINVAL, "null")
+    err(L.ocs_activate(P, 100000, 7, 0.5, b"--precision=tc-fp16", P, 1 << 30, ctypes.byref(n_out)),
+        ocs_lib.OCS_EINVAL, "2^8 .. 2^12")
+    err(L.ocs_activate(P, 100000, 12, 0.5, b"--precision=tc-bf16x3", P, 1 << 30, ctypes.byref(n_out)),
+        ocs_lib.OCS_EINVAL, "does not fit")
+    # a negative overlap ratio (accepted, as in the reference) advances frames by more than N
+    assert ocs_lib.geometry(100000, 8, -0.5, "").hop == 384
+    err(L.ocs_activate(P, 100000, 8, -0.5, b"--precision=tc-bf16x2", P, 1 << 30, ctypes.byref(n_out)),
+        ocs_lib.OCS_EINVAL, "frame advance")
+    err(L.ocs_activate(P, 0, 10, 0.5, b"", P, 1 << 30, ctypes.byref(n_out)), ocs_lib.OCS_EINVAL, "empty")
+    err(L.ocs_activate(P, 100000, 10, 0.5, b"--gaussian_window=4<<sigma", P, 1 << 30, ctypes.byref(n_out)),
+        ocs_lib.OCS_EPIPELINE, "--gaussian_window")
+    # batches and the server
+    err(L.ocs_batch_device(None, 3, None), ocs_lib.OCS_EINVAL, "bad request list")
+    err(L.ocs_batch_prepare(None, -1), ocs_lib.OCS_EINVAL, "bad request list")
+    err(L.ocs_batch_device_noalloc(None, 300, None), ocs_lib.OCS_EINVAL, "bad request list")
+    t = ctypes.c_uint64()
+    err(L.ocs_server_submit(P, 1000, 10, 0.5, b"", P, 1 << 20, ctypes.byref(t)), ocs_lib.OCS_EINVAL, "not running")
+    err(L.ocs_server_wait(1, 0, None), ocs_lib.OCS_EINVAL, "not running")
+    err(L.ocs_server_stop(), ocs_lib.OCS_EINVAL, "not running")
