@@ -19,6 +19,9 @@
 //                 every result correct (run under ThreadSanitizer, this also
 //                 checks the shared plan, window, tuning and slot state)
 //   batch         ocs_batch_device over mixed requests, windows 2^6 .. 2^16
+//   capture_tune  ocs_activate_device on a capturing stream never times
+//                 kernel variants (no event is made, nothing synchronises);
+//                 it runs before any check that tunes other keys
 //   capture       a captured batch keeps its own descriptor buffers: a later
 //                 batch does not touch them; a capture without a preceding
 //                 ocs_batch_prepare is refused
@@ -362,6 +365,38 @@ void capture()
     std::printf("ok %s (%zu captured uploads)\n", name, snap.size());
 }
 
+void capture_tune()
+{
+    const char* name = "capture_tune";
+    setenv("OCS_AUTOTUNE", "1", 1);
+    cudaStream_t cap;
+    check(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) == cudaSuccess, name, "stream");
+    // a window and size class not tuned before: outside a capture this request would time variants
+    std::vector<float> x = make_signal(700000, 77);
+    const char* opts = "--nuttall_window --half_complex_return";
+    ocs_geometry g;
+    check(ocs_geometry_get(x.size(), 9, 0.25f, opts, &g) == OCS_OK, name, "geometry");
+    float* d_in = nullptr;
+    float* d_out = nullptr;
+    check(cudaMalloc(&d_in, x.size() * 4) == cudaSuccess && cudaMalloc(&d_out, g.out_floats * 4) == cudaSuccess, name,
+          "alloc");
+    std::memcpy(d_in, x.data(), x.size() * 4);
+    fake::capturing = cap;
+    fake::event_fail_after = 0;  // a timing attempt would fail the call
+    const int rc = ocs_activate_device(d_in, x.size(), 9, 0.25f, opts, d_out, g.out_floats, cap);
+    fake::event_fail_after = -1;
+    fake::capturing = nullptr;
+    check(rc == OCS_OK, name, "rc " + std::to_string(rc));
+    cudaStreamSynchronize(cap);
+    check(std::memcmp(d_out, expected_out(x.data(), x.size(), 9, 0.25f, opts).data(), g.out_floats * 4) == 0, name,
+          "result");
+    cudaFree(d_in);
+    cudaFree(d_out);
+    cudaStreamDestroy(cap);
+    setenv("OCS_AUTOTUNE", "0", 1);
+    std::printf("ok %s\n", name);
+}
+
 void shutdown()
 {
     const char* name = "shutdown";
@@ -429,6 +464,7 @@ int main(int argc, char** argv)
     table_fail();
     slot_fail();
     tune_fail();
+    capture_tune();  // before any check that tunes other keys
     activate();
     concurrent();
     batch();

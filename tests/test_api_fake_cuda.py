@@ -25,7 +25,8 @@ CSRC = os.path.join(ROOT, "occastft_gb300", "csrc")
 SOURCES = [os.path.join(CSRC, "ocs_api.cpp"), os.path.join(CSRC, "ocs_host.cpp"),
            os.path.join(FAKE, "fake_runtime.cpp"), os.path.join(FAKE, "fake_kernels.cpp"),
            os.path.join(FAKE, "api_stress.cpp")]
-CHECKS = ["setup_fail", "table_fail", "slot_fail", "tune_fail", "activate", "concurrent", "batch", "capture", "shutdown"]
+CHECKS = ["setup_fail", "table_fail", "slot_fail", "tune_fail", "capture_tune", "activate", "concurrent", "batch",
+          "capture", "shutdown"]
 
 
 def _build(out, sanitize):
