@@ -214,6 +214,34 @@ def cpu_reference_impl():
         "oracle port of the reference OpenMP runner (bit-exact to it), OpenMP over all host cores"
 
 
+def cpu_serial_baseline(sample_n: int = 1 << 21, budget_s: float = 3.0) -> dict:
+    """The reference's Serial runner on one host core, on a bounded sample of
+    the same workload: its own code built from source where present, else the
+    oracle port of it (bit-exact) with one thread."""
+    from oracle import orc
+
+    if orc.RefLib.available("libref_serial.so"):
+        R = orc.RefLib("libref_serial.so")
+        kind, desc = "reference", "reference Serial runner (StandAlone/cross_gpgpu/Serial) built -O2 from source"
+        fn = lambda x: R.activate(x, HEAD_EXP, HEAD_OV, HEAD_OPTS)[0]  # noqa: E731
+    else:
+        orc.lib()
+        kind, desc = "port", "oracle port of the reference Serial runner (bit-exact to it)"
+        fn = lambda x: orc.serial_pipeline(x, HEAD_EXP, HEAD_OV, HEAD_OPTS, nthreads=1)  # noqa: E731
+    x = make_signal_np(sample_n)
+    fn(x)  # warm
+    times = []
+    t_end = time.time() + budget_s
+    while time.time() < t_end or len(times) < 3:
+        t0 = time.perf_counter()
+        fn(x)
+        times.append(time.perf_counter() - t0)
+    med = statistics.median(times)
+    return {"value": sample_n / med / 1e9, "unit": METRIC, "cores": 1, "kind": kind,
+            "sample": f"first {sample_n} samples of the 1e8 signal, same options; median of {len(times)} runs; "
+                      f"{desc}, one thread"}
+
+
 def cpu_baseline(sample_n: int = 1 << 23, budget_s: float = 12.0):
     kind, fn, desc = cpu_reference_impl()
     x = make_signal_np(sample_n)
@@ -227,7 +255,8 @@ def cpu_baseline(sample_n: int = 1 << 23, budget_s: float = 12.0):
     med = statistics.median(times)
     return {"value": sample_n / med / 1e9, "unit": METRIC, "cores": os.cpu_count(), "kind": kind,
             "sample": f"first {sample_n} samples of the 1e8 signal, N=1024 Hamming ov 0.5 power; "
-                      f"median of {len(times)} runs; {desc}"}
+                      f"median of {len(times)} runs; {desc}",
+            "serial_1core": cpu_serial_baseline()}
 
 
 def run_reference_arm(args):

@@ -34,3 +34,20 @@ def test_fp32_pipe_bound():
     b = bench.fp32_pipe_bound(2048, 10**6, 1e-3, 152, 2000.0)
     assert b["gflop_s"] / a["gflop_s"] == pytest.approx(2 * 10 / 9, rel=1e-6)
     assert math.isclose(bench.NOMINAL_SM_MAX_MHZ, 2070.0)
+
+
+@pytest.mark.parametrize("have_reference_build", [True, False])
+def test_serial_one_core_baseline(monkeypatch, have_reference_build):
+    """cpu_baseline's single-core Serial figure: the reference's own Serial code
+    where it was built from source, else the bit-exact port on one thread
+    (the GPU machine, where the reference checkout is absent)."""
+    from oracle import orc
+
+    if not have_reference_build:
+        monkeypatch.setattr(orc.RefLib, "available", staticmethod(lambda name="libref_serial.so": False))
+    elif not orc.RefLib.available("libref_serial.so"):
+        pytest.skip("oracle/_ref not built")
+    r = bench.cpu_serial_baseline(sample_n=1 << 16, budget_s=0.2)
+    assert r["cores"] == 1 and r["unit"] == bench.METRIC and r["value"] > 0
+    assert r["kind"] == ("reference" if have_reference_build else "port")
+    assert "one thread" in r["sample"]
