@@ -51,3 +51,28 @@ def test_serial_one_core_baseline(monkeypatch, have_reference_build):
     assert r["cores"] == 1 and r["unit"] == bench.METRIC and r["value"] > 0
     assert r["kind"] == ("reference" if have_reference_build else "port")
     assert "one thread" in r["sample"]
+
+
+def test_reference_arm_prints_its_line():
+    """`bench.py --impl reference` (the reference's CPU implementation of the
+    path, timed on the host cores) prints one JSON line with the keys of the
+    bench contract; warm-up is never below three steps."""
+    import json
+    import os
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "0"], capture_output=True, text=True, timeout=600, cwd=root)
+    assert r.returncode == 0, r.stderr[-3000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC and d["unit"] == bench.METRIC
+    assert d["value"] > 0 and d["higher_is_better"] is True and d["n_gpus"] == 1
+    assert d["steps"] == 1 and d["warmup"] >= 3
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["config"]["window"] == 1024 and d["config"]["overlap"] == 0.5
