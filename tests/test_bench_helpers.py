@@ -40,7 +40,7 @@ def test_fp32_pipe_bound():
 def test_serial_one_core_baseline(monkeypatch, have_reference_build):
     """cpu_baseline's single-core Serial figure: the reference's own Serial code
     where it was built from source, else the bit-exact port on one thread
-    (the GPU machine, where the reference checkout is absent)."""
+    (on machines without the reference checkout)."""
     from oracle import orc
 
     if not have_reference_build:
