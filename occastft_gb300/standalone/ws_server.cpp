@@ -183,6 +183,7 @@ bool handshake(int fd)
 }
 
 constexpr uint64_t kMaxMessage = 1ull << 36;
+constexpr uint64_t kRecvStep = 64ull << 20;  // payload bytes received per buffer growth
 
 }  // namespace
 
@@ -358,20 +359,36 @@ void WsServer::serve(int fd, const Handler& on_message)
             // with a 64-bit frame length could); an allocation the host
             // cannot make is answered like a message that is too big
             bool fits = len <= kMaxMessage && have <= kMaxMessage - len;
-            if (fits) {
+            // The buffer grows with the bytes that arrive, not with the
+            // length a header states: a header alone allocates nothing.
+            // Capacity doubles, capped at the frame's end, so the copies on
+            // growth stay within twice the message.
+            bool lost = false;
+            for (uint64_t got = 0; fits && got < len;) {
+                const uint64_t step = std::min<uint64_t>(len - got, kRecvStep);
+                const size_t words = (size_t)((have + got + step + 7) / 8);
                 try {
-                    msg.store.resize((have + len + 7) / 8);
+                    if (words > msg.store.capacity())
+                        msg.store.reserve(std::max<size_t>(
+                            words, std::min<size_t>(2 * msg.store.capacity(), (size_t)((have + len + 7) / 8))));
+                    msg.store.resize(words);
                 } catch (const std::bad_alloc&) {
                     fits = false;
+                    break;
                 }
+                if (!recv_all(fd, reinterpret_cast<uint8_t*>(msg.store.data()) + have + got, (size_t)step)) {
+                    lost = true;
+                    break;
+                }
+                got += step;
             }
             if (!fits) {
                 const uint8_t code[2] = {0x03, 0xF1};  // 1009 message too big
                 conn.send_frame(8, code, 2);
                 break;
             }
+            if (lost) break;
             uint8_t* dst = reinterpret_cast<uint8_t*>(msg.store.data()) + have;
-            if (len && !recv_all(fd, dst, (size_t)len)) break;
             // unmask; the key repeats every 4 bytes of the frame payload
             uint64_t i = 0;
             uint32_t k32;

@@ -155,6 +155,35 @@ def test_oversized_continuation_frame_is_refused(runner, length):
     other.close()
 
 
+def _rss_mb(pid):
+    for line in open(f"/proc/{pid}/status"):
+        if line.startswith("VmRSS:"):
+            return int(line.split()[1]) / 1024
+    return 0.0
+
+
+def test_frame_header_alone_allocates_nothing(runner):
+    """A header that states an 8 GB payload, followed by 1 MB of it: the
+    runner's buffer grows with the bytes that arrive (64 MB steps), so its
+    resident memory stays far below the stated length.  Dropping the
+    connection mid-frame ends only that connection."""
+    import time
+
+    p, port = runner
+    before = _rss_mb(p.pid)
+    ws = proxy.WsClient("127.0.0.1", port)
+    mask = b"\x05\x06\x07\x08"
+    ws.sock.sendall(bytes([0x82, 0x80 | 127]) + struct.pack(">Q", 8 << 30) + mask + bytes(1 << 20))
+    time.sleep(0.5)
+    grown = _rss_mb(p.pid) - before
+    assert grown < 256, f"runner grew by {grown:.0f} MB on a header alone"
+    ws.sock.close()
+    other = proxy.WsClient("127.0.0.1", port)
+    other.ping(b"after")
+    assert other.recv(timeout=30) == (10, b"after")
+    other.close()
+
+
 def test_close_request_stops_runner():
     p, port = cu.start_cudarun()
     try:
