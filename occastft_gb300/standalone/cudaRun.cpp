@@ -105,6 +105,8 @@ void handle_request(Connection& c, const Message& m)
         path = "shm";
         if (q.sharedMemory == "ERR") {
             status = "request marked ERR";
+        } else if (!protocol_shm_name(q.sharedMemory)) {
+            status = "shared memory name is not of the form /STFT<mappedID>SHAREDMEM";
         } else {
             ShmMapping map;
             status = shm_map(q.sharedMemory, q.overlapdataLength, map, g_shm_mode == ShmMode::populate);

@@ -12,6 +12,13 @@
 
 namespace ocs_standalone {
 
+bool protocol_shm_name(const std::string& name)
+{
+    static const std::string head = "/STFT", tail = "SHAREDMEM";
+    return name.size() > head.size() + tail.size() && name.compare(0, head.size(), head) == 0 &&
+           name.compare(name.size() - tail.size(), tail.size(), tail) == 0 && name.find('/', 1) == std::string::npos;
+}
+
 size_t page_rounded_bytes(uint64_t floats)
 {
     const uint64_t page = (uint64_t)sysconf(_SC_PAGESIZE);

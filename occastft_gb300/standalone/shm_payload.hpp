@@ -19,6 +19,11 @@ struct ShmMapping {
     int fd = -1;
 };
 
+// Whether `name` has the protocol's form "/STFT<mappedID>SHAREDMEM" (no other
+// '/').  The runner maps only such objects: a peer cannot point it at, and
+// have it overwrite, any other shared-memory object its user can open.
+bool protocol_shm_name(const std::string& name);
+
 // page-rounded byte size of `floats` floats (FFTStruct.hpp:151-157)
 size_t page_rounded_bytes(uint64_t floats);
 

@@ -214,3 +214,26 @@ def test_proxy_remote_server(served, ocs_lib):
             assert got is not None and np.array_equal(got, want), (exp, ov, opts)
     finally:
         p.ws.close()  # the shared runner keeps serving the other tests
+
+
+def test_foreign_shared_memory_object_is_not_touched(served):
+    """A request naming a shared-memory object outside the protocol's
+    "/STFT<mappedID>SHAREDMEM" form is answered "ERR" and the object is
+    neither read nor written."""
+    from multiprocessing import shared_memory
+
+    seg = shared_memory.SharedMemory(name=f"ocs_foreign_{os.getpid()}", create=True, size=1 << 20)
+    try:
+        view = np.ndarray((1 << 18,), dtype=np.float32, buffer=seg.buf)
+        view[:] = 3.25
+        x = signal(5, 100_000)
+        req = wire.Request(windowRadix=10, overlapRatio=0.5, mappedID="x", sharedMemory="/" + seg.name,
+                           dataLength=x.size, overlapdataLength=proxy.to_overlap_length(x.size, 0.5, 1024),
+                           options="", posixFileDes=-1)
+        a = _ask(served, req)
+        assert a.sharedMemory == "ERR"
+        assert np.all(view == 3.25)
+        del view
+    finally:
+        seg.close()
+        seg.unlink()
