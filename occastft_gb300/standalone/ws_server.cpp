@@ -6,6 +6,7 @@
 #include <netinet/tcp.h>
 #include <poll.h>
 #include <sys/socket.h>
+#include <sys/time.h>
 #include <unistd.h>
 
 #include <algorithm>
@@ -183,6 +184,7 @@ bool handshake(int fd)
 }
 
 constexpr uint64_t kMaxMessage = 1ull << 36;
+constexpr int kHandshakeSeconds = 5;  // a peer that has not sent its opening request by then is dropped
 constexpr uint64_t kRecvStep = 64ull << 20;  // payload bytes received per buffer growth
 
 }  // namespace
@@ -276,6 +278,10 @@ void WsServer::run(const Handler& on_message)
         if (r <= 0 || !(p.revents & POLLIN)) continue;
         const int fd = ::accept(lfd_, nullptr, nullptr);
         if (fd < 0) continue;
+        if (workers.size() >= (size_t)kMaxConnections) {  // at the cap: refused at once
+            ::close(fd);
+            continue;
+        }
         int one = 1;
         ::setsockopt(fd, IPPROTO_TCP, TCP_NODELAY, &one, sizeof one);
         {
@@ -305,7 +311,14 @@ void WsServer::run(const Handler& on_message)
 void WsServer::serve(int fd, const Handler& on_message)
 {
     Connection conn(fd);
-    if (handshake(fd)) {
+    // the opening handshake has a deadline; afterwards reads wait as long as
+    // the peer keeps the connection open
+    timeval tv{kHandshakeSeconds, 0};
+    ::setsockopt(fd, SOL_SOCKET, SO_RCVTIMEO, &tv, sizeof tv);
+    const bool upgraded = handshake(fd);
+    tv = timeval{0, 0};
+    ::setsockopt(fd, SOL_SOCKET, SO_RCVTIMEO, &tv, sizeof tv);
+    if (upgraded) {
         Message msg;
         bool in_msg = false;
         uint64_t have = 0;

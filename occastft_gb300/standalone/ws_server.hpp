@@ -8,7 +8,10 @@
 // messages, ping/pong, close, and unmasked server frames.  Extensions that a
 // client offers (permessage-deflate) are declined by not echoing them, which
 // RFC 7692 allows; the client then sends uncompressed frames.  One thread
-// per connection; messages of one connection are handled in order.
+// per connection; messages of one connection are handled in order.  At most
+// kMaxConnections connections are open at once (more are closed at
+// accept), and a peer must complete its opening handshake within a few
+// seconds.
 #pragma once
 #include <atomic>
 #include <cstddef>
@@ -18,6 +21,8 @@
 #include <vector>
 
 namespace ocs_standalone {
+
+constexpr int kMaxConnections = 256;
 
 // SHA-1 (FIPS 180-4) and base64 (RFC 4648), as the handshake needs them.
 void sha1(const uint8_t* data, size_t len, uint8_t out[20]);

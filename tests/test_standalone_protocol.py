@@ -184,6 +184,50 @@ def test_frame_header_alone_allocates_nothing(runner):
     other.close()
 
 
+def test_silent_peer_is_dropped_after_the_handshake_deadline(runner):
+    """A peer that connects and never sends its opening request is closed
+    after the handshake deadline (5 s) instead of holding a thread."""
+    import time
+
+    _, port = runner
+    with socket.create_connection(("127.0.0.1", port), timeout=30) as s:
+        t0 = time.time()
+        assert s.recv(16) == b""  # closed by the runner
+        assert 3 < time.time() - t0 < 20
+
+
+def test_connections_beyond_the_cap_are_refused(runner):
+    """At most 256 connections are open at once: the ones beyond are closed at
+    accept, the others stay open, and a clean client is served once they go."""
+    _, port = runner
+    # upgraded connections: the handshake deadline does not apply to them
+    held = [proxy.WsClient("127.0.0.1", port) for _ in range(256)]
+    try:
+        extra = [socket.create_connection(("127.0.0.1", port), timeout=10) for _ in range(8)]
+        for s in extra:
+            s.settimeout(3)
+            assert s.recv(16) == b""  # refused at once, well before the handshake deadline
+            s.close()
+        held[0].ping(b"held")
+        assert held[0].recv(timeout=10) == (10, b"held")  # still served
+    finally:
+        for ws in held:
+            ws.close()
+    import time
+
+    deadline = time.time() + 20
+    while True:  # the runner reaps the closed connections' threads
+        try:
+            ws = proxy.WsClient("127.0.0.1", port)
+            break
+        except (OSError, ConnectionError):
+            assert time.time() < deadline
+            time.sleep(0.2)
+    ws.ping(b"back")
+    assert ws.recv(timeout=30) == (10, b"back")
+    ws.close()
+
+
 def test_close_request_stops_runner():
     p, port = cu.start_cudarun()
     try:
