@@ -154,9 +154,16 @@ int ocs_batch_device(ocs_request* reqs, int count, void* stream);
  * GPU that loads the library until the process exits.  Limits (rejected with
  * OCS_ENOMEM and a message): at most 256 requests per call, windows 2^6..2^13,
  * distinct window tables of one call within the array's window region.
- * Requests with larger windows get status OCS_EINVAL.  The first call on a
- * device (with that device current) sets the array up and synchronizes
- * `stream` once.  Calls cannot be captured into a CUDA graph (OCS_EINVAL):
+ * Requests with larger windows, or with a --precision=tc-* option (the
+ * tensor-core forms need tables the array has no room for), get status
+ * OCS_EINVAL.  When a call fails with OCS_ENOMEM, every request it accepted
+ * gets that status too (nothing was launched).  The first call on a device
+ * (with that device current) sets the array up and synchronizes `stream`
+ * once; CUDA loads the library's device code lazily, so that is also when
+ * the array takes its device memory: call once with count = 0 (set-up only)
+ * before an allocator of your own reserves the device.  ocs_shutdown forgets
+ * the set-up, so a call after a device reset sets it up again.
+ * Calls cannot be captured into a CUDA graph (OCS_EINVAL):
  * their descriptors go through a host staging buffer that every call
  * rewrites.  All calls share the array: calls whose work overlaps on the GPU
  * race, so order them on one stream or with events. */

@@ -689,9 +689,17 @@ int batch_build(ocs_request* reqs, int count, BatchPlan& bp, bool write_status)
                 rc = get_twiddles(r.exp, true, &twp);
             }
         }
+        // the tensor-core forms build their DFT tables before a capture can need them
+        if (!rc && r.opt.precision >= 1) {
+            const cudaError_t te = ocs::tc_prepare(r.exp, r.opt.precision);
+            if (te != cudaSuccess) rc = cuda_fail(te, "tensor-core tables");
+        }
         if (write_status) q.status = rc;
         if (rc) continue;
-        if (ocs::batch_supports(r.exp)) order.push_back(i);
+        // requests that ask for a tensor-core precision get their own launch
+        // of that form (the batch kernel is the FP32 form), as do windows
+        // above the batch kernel's range
+        if (ocs::batch_supports(r.exp) && r.opt.precision == 0) order.push_back(i);
         else bp.big.push_back(i);
     }
     auto outk_of = [&](int i) {
@@ -913,6 +921,7 @@ int ocs_init(int device)
 
 void ocs_shutdown(void)
 {
+    ocs::internal::noalloc_forget_devices();
     Context& c = ctx();
     std::lock_guard<std::mutex> lk(c.mu);
     if (!c.ready) return;

@@ -26,6 +26,8 @@ void batch_scratch_release(BatchScratch& b);
 int batch_prepare_into(const ocs_request* reqs, int count, BatchScratch& b);
 int batch_enqueue(ocs_request* reqs, int count, cudaStream_t st, BatchScratch& b);
 int ensure_ready();
+// drops the no-allocation batch's per-device set-up (ocs_shutdown)
+void noalloc_forget_devices();
 void set_error(int code, const std::string& msg);
 
 }  // namespace internal

@@ -137,6 +137,9 @@ bool tc_mode_supported(int exp, int pm);
 bool tc_piped(int exp, uint64_t hop);
 cudaError_t launch_tc(int exp, int outk, int pm, const FusedArgs& a, int* err, int test_stall, int sms,
                       cudaStream_t st);
+// builds the DFT-matrix and twiddle tables the form (exp, pm) uses, once per
+// device, so that a later launch (possibly under stream capture) finds them
+cudaError_t tc_prepare(int exp, int pm);
 
 // unfused per-stage kernels behind the runnerFunction hooks
 cudaError_t launch_overlap(const float* in, uint32_t ofull, uint32_t n, uint32_t exp, uint32_t hop,

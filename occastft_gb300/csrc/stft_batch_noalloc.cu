@@ -24,7 +24,12 @@
 //
 // Set-up: the first call on a device (with that device current) takes the
 // array's device address with cudaGetSymbolAddress, fills the twiddle tables
-// of every supported window size into it and waits for that to finish.
+// of every supported window size into it and waits for that to finish.  CUDA
+// loads a library's device code lazily, so that first call is also when the
+// array and this file's kernels take their device memory: a caller whose own
+// allocator will reserve the device should make one call with count = 0 (it
+// does the set-up and nothing else) before it does.  ocs_shutdown forgets
+// the set-up, so a call after a device reset sets the device up again.
 //
 // Calls are not capturable into a CUDA graph (refused with OCS_EINVAL): a
 // replay would upload whatever descriptors the host staging buffer holds
@@ -226,6 +231,19 @@ int setup_locked(int dev, cudaStream_t st)
 
 }  // namespace
 
+namespace ocs {
+namespace internal {
+// Forgets the per-device set-up (called by ocs_shutdown): after a
+// cudaDeviceReset the module is loaded again, possibly at another address,
+// and its tables are gone, so the next call sets the device up afresh.
+void noalloc_forget_devices()
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    for (DeviceSetup& d : g_dev) d = DeviceSetup{};
+}
+}  // namespace internal
+}  // namespace ocs
+
 extern "C" int ocs_batch_device_noalloc(ocs_request* reqs, int count, void* stream)
 {
     if (count < 0 || (count > 0 && !reqs)) return fail(OCS_EINVAL, "bad request list");
@@ -269,6 +287,9 @@ extern "C" int ocs_batch_device_noalloc(ocs_request* reqs, int count, void* stre
             s = ocs::make_geometry(q.n, q.window_size_exp, q.overlap_ratio, it.o, it.g);
             if (s != "OK") st_i = OCS_EINVAL;
             else if (q.window_size_exp > kMaxExp) st_i = OCS_EINVAL;
+            // the tensor-core forms keep tables this array has no room for:
+            // refused rather than silently run in FP32
+            else if (it.o.precision != 0) st_i = OCS_EINVAL;
             else if (q.out_cap < it.g.out_floats) st_i = OCS_ESPACE;
             else if (!q.in || !q.out) st_i = OCS_EINVAL;
         }
@@ -303,9 +324,12 @@ extern "C" int ocs_batch_device_noalloc(ocs_request* reqs, int count, void* stre
             if (wins[j].kind == kind && wins[j].exp == it.exp && std::memcmp(&wins[j].sigma, &sigma, 4) == 0) w = j;
         if (w < 0) {
             const size_t bytes = ((size_t)4 << it.exp);
-            if (woff + bytes > kScratchBytes)
+            if (woff + bytes > kScratchBytes) {
+                // nothing is launched: no request of this call gets a result
+                for (int j = 0; j < ni; ++j) reqs[items[j].idx].status = OCS_ENOMEM;
                 return fail(OCS_ENOMEM, "no-allocation batch: distinct window tables exceed " +
                                             std::to_string(kWindowBytes) + " bytes");
+            }
             float* dst = reinterpret_cast<float*>(g_host_stage + woff);
             if (kind == ocs::WIN_NONE) {
                 for (int i = 0; i < (1 << it.exp); ++i) dst[i] = 0.5f;
@@ -338,7 +362,10 @@ extern "C" int ocs_batch_device_noalloc(ocs_request* reqs, int count, void* stre
         hreq[k] = r;
     }
     if (ni == 0) return OCS_OK;
-    if (tiles >= 0xffffffffull) return fail(OCS_ENOMEM, "no-allocation batch: too many tiles in one call");
+    if (tiles >= 0xffffffffull) {
+        for (int j = 0; j < ni; ++j) reqs[items[j].idx].status = OCS_ENOMEM;
+        return fail(OCS_ENOMEM, "no-allocation batch: too many tiles in one call");
+    }
     uint32_t* hdr = reinterpret_cast<uint32_t*>(g_host_stage);
     hdr[0] = 0;  // the tile counter must start at zero on every call
     hdr[1] = (uint32_t)tiles;

@@ -1555,6 +1555,21 @@ bool tc_mode_supported(int exp, int pm)
 // the generic form (2^9, 2^11, 2^12) takes any advance
 bool tc_piped(int exp, uint64_t hop) { return (exp != 8 && exp != 10) || hop <= (1ull << exp); }
 
+cudaError_t tc_prepare(int exp, int pm)
+{
+    cudaError_t e = cudaSuccess;
+    if (exp == 8) {
+        if (pm == PM_BF16X2) tc_tables<16, PM_BF16X2>(&e);
+        else if (pm == PM_BF16X3) tc_tables<16, PM_BF16X3>(&e);
+        else tc_tables<16, PM_FP16X2>(&e);
+    } else if (exp == 10) {
+        if (pm == PM_BF16X2) tc_tables<32, PM_BF16X2>(&e);
+        else if (pm == PM_BF16X3) tc_tables<32, PM_BF16X3>(&e);
+        else tc_tables<32, PM_FP16X2>(&e);
+    }
+    return e;  // the generic form (2^9, 2^11, 2^12) builds its tables in each CTA
+}
+
 cudaError_t launch_tc(int exp, int outk, int pm, const FusedArgs& a, int* err, int test_stall, int sms,
                       cudaStream_t st)
 {

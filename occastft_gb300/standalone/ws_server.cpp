@@ -6,11 +6,12 @@
 #include <netinet/tcp.h>
 #include <poll.h>
 #include <sys/socket.h>
-#include <sys/time.h>
 #include <unistd.h>
 
 #include <algorithm>
 #include <cctype>
+#include <cerrno>
+#include <chrono>
 #include <cstring>
 #include <exception>
 #include <memory>
@@ -142,14 +143,26 @@ std::string trim(const std::string& s)
     return s.substr(a, b - a);
 }
 
-// the opening handshake; false when the peer is not a WebSocket client
-bool handshake(int fd)
+// the opening handshake; false when the peer is not a WebSocket client or
+// has not sent its whole opening request by `deadline` (one limit for all
+// reads, so a peer that trickles bytes cannot stretch it)
+bool handshake(int fd, std::chrono::steady_clock::time_point deadline)
 {
     std::string req;
     char buf[1024];
     while (req.find("\r\n\r\n") == std::string::npos) {
         if (req.size() > 16384) return false;
+        const auto left = std::chrono::duration_cast<std::chrono::milliseconds>(
+                              deadline - std::chrono::steady_clock::now())
+                              .count();
+        if (left <= 0) return false;
+        pollfd p{fd, POLLIN, 0};
+        const int r = ::poll(&p, 1, (int)std::min<long long>(left, 1000));
+        if (r < 0 && errno == EINTR) continue;
+        if (r < 0) return false;
+        if (r == 0) continue;  // the loop re-checks the deadline
         const ssize_t k = ::recv(fd, buf, sizeof buf, 0);
+        if (k < 0 && errno == EINTR) continue;
         if (k <= 0) return false;
         req.append(buf, (size_t)k);
     }
@@ -278,6 +291,7 @@ void WsServer::run(const Handler& on_message)
         if (r <= 0 || !(p.revents & POLLIN)) continue;
         const int fd = ::accept(lfd_, nullptr, nullptr);
         if (fd < 0) continue;
+        const auto accepted = std::chrono::steady_clock::now();
         if (workers.size() >= (size_t)kMaxConnections) {  // at the cap: refused at once
             ::close(fd);
             continue;
@@ -290,8 +304,8 @@ void WsServer::run(const Handler& on_message)
         }
         auto done = std::make_shared<std::atomic<bool>>(false);
         try {
-            workers.push_back(Worker{std::thread([this, fd, &on_message, done] {
-                                         serve(fd, on_message);
+            workers.push_back(Worker{std::thread([this, fd, accepted, &on_message, done] {
+                                         serve(fd, accepted, on_message);
                                          done->store(true);
                                      }),
                                      done});
@@ -308,16 +322,15 @@ void WsServer::run(const Handler& on_message)
     for (auto& w : workers) w.t.join();
 }
 
-void WsServer::serve(int fd, const Handler& on_message)
+void WsServer::serve(int fd, std::chrono::steady_clock::time_point accepted, const Handler& on_message)
 {
     Connection conn(fd);
-    // the opening handshake has a deadline; afterwards reads wait as long as
-    // the peer keeps the connection open
-    timeval tv{kHandshakeSeconds, 0};
-    ::setsockopt(fd, SOL_SOCKET, SO_RCVTIMEO, &tv, sizeof tv);
-    const bool upgraded = handshake(fd);
-    tv = timeval{0, 0};
-    ::setsockopt(fd, SOL_SOCKET, SO_RCVTIMEO, &tv, sizeof tv);
+    // the whole opening handshake must arrive within kHandshakeSeconds of
+    // the accept; afterwards reads wait as long as the peer keeps the
+    // connection open (a client such as the reference's proxy holds one
+    // connection and sends requests on it whenever it has one)
+    const bool upgraded =
+        handshake(fd, accepted + std::chrono::seconds(kHandshakeSeconds));
     if (upgraded) {
         Message msg;
         bool in_msg = false;

@@ -11,9 +11,10 @@
 // per connection; messages of one connection are handled in order.  At most
 // kMaxConnections connections are open at once (more are closed at
 // accept), and a peer must complete its opening handshake within a few
-// seconds.
+// seconds of the accept (one limit for all its reads).
 #pragma once
 #include <atomic>
+#include <chrono>
 #include <cstddef>
 #include <cstdint>
 #include <functional>
@@ -66,7 +67,8 @@ public:
     int port() const { return port_; }
 
 private:
-    void serve(int fd, const Handler& on_message);
+    // accepted: when the connection was accepted (the handshake deadline counts from it)
+    void serve(int fd, std::chrono::steady_clock::time_point accepted, const Handler& on_message);
     int lfd_ = -1;
     int port_ = 0;
     std::atomic<bool> stopping_{false};

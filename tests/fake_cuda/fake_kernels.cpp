@@ -122,6 +122,7 @@ cudaError_t launch_tc(int exp, int outk, int, const FusedArgs& a, int*, int, int
 {
     return fused_like(exp, outk, a, st);
 }
+cudaError_t tc_prepare(int, int) { return cudaSuccess; }
 
 cudaError_t launch_overlap(const float*, uint32_t, uint32_t, uint32_t, uint32_t, float*, cudaStream_t)
 {
@@ -132,4 +133,11 @@ cudaError_t launch_remove_dc(float*, uint32_t, uint32_t, cudaStream_t) { return 
 cudaError_t launch_half_complex(float*, const float*, const float*, uint32_t, cudaStream_t) { return no_work(); }
 cudaError_t launch_to_power(float*, const float*, const float*, uint32_t, cudaStream_t) { return no_work(); }
 
+}  // namespace ocs
+
+namespace ocs {
+namespace internal {
+// the no-allocation batch (a .cu file) is not part of the host stand-in build
+void noalloc_forget_devices() {}
+}  // namespace internal
 }  // namespace ocs

@@ -95,6 +95,34 @@ def test_per_request_errors(ocs_lib, orc):
     assert orc.rel_l2(outs[0].cpu().numpy(), orc.fp64_stft(x, 8, 0.5, "--hanning_window")) <= REL_L2
 
 
+def test_tensor_core_precision_is_honoured_in_batches(ocs_lib, orc):
+    """A request that asks for a tensor-core form gets that form in a batch
+    (its own launch beside the persistent FP32 launch): the same bits as the
+    single-request call with the same options, not the FP32 result."""
+    items = [(signal(40, 70000), 10, 0.75, "--hanning_window --precision=tc-fp16"),
+             (signal(41, 50000), 9, 0.5, "--hamming_window"),
+             (signal(42, 90000), 12, 0.5, "--blackman_window --half_complex_return --precision=tc-bf16x2")]
+    import torch
+
+    st, outs, bufs = _run_batch(ocs_lib, items)
+    assert st == [0, 0, 0]
+    for (x, exp, ov, opts), out, (d_in, _, g) in zip(items, outs, bufs):
+        got = out[: g.out_floats]
+        d_single = torch.empty(g.out_floats, device="cuda")
+        ocs_lib.activate_device(d_in, x.size, exp, ov, opts, d_single, g.out_floats)
+        torch.cuda.synchronize()
+        single = d_single.cpu().numpy()
+        if "--precision" in opts:
+            assert np.array_equal(got, single), opts
+        else:  # the batch kernel and the single-request kernel may differ in rounding
+            assert orc.rel_l2(got, single) <= REL_L2, opts
+        tol = 1e-4 if "bf16x2" in opts else REL_L2
+        assert orc.rel_l2(got, orc.fp64_stft(x, exp, ov, opts)) <= tol, opts
+    # the tensor-core result differs from the FP32 one: the form really ran
+    fp32 = ocs_lib.activate(items[0][0], 10, 0.75, "--hanning_window")
+    assert not np.array_equal(outs[0][: bufs[0][2].out_floats], fp32)
+
+
 def test_batch_cuda_graph_capture(ocs_lib):
     import torch
 

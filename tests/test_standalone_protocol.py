@@ -196,6 +196,34 @@ def test_silent_peer_is_dropped_after_the_handshake_deadline(runner):
         assert 3 < time.time() - t0 < 20
 
 
+def test_trickling_peer_is_dropped_at_the_handshake_deadline(runner):
+    """A peer that sends its opening request one byte a second is closed
+    about 5 s after the accept: the deadline covers the whole handshake, not
+    each read."""
+    import time
+
+    _, port = runner
+    req = b"GET / HTTP/1.1\r\nHost: x\r\nUpgrade: websocket\r\nConnection: Upgrade\r\n"
+    with socket.create_connection(("127.0.0.1", port), timeout=30) as s:
+        t0 = time.time()
+        closed_at = None
+        for b in req:
+            try:
+                s.sendall(bytes([b]))
+            except OSError:
+                closed_at = time.time()
+                break
+            s.settimeout(1.0)
+            try:
+                if s.recv(16) == b"":
+                    closed_at = time.time()
+                    break
+            except socket.timeout:
+                pass
+        assert closed_at is not None, "the runner kept a trickling peer past its handshake deadline"
+        assert 3 < closed_at - t0 < 9
+
+
 def test_connections_beyond_the_cap_are_refused(runner):
     """At most 256 connections are open at once: the ones beyond are closed at
     accept, the others stay open, and a clean client is served once they go."""

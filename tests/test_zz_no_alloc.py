@@ -86,3 +86,62 @@ def test_noalloc_rejects_oversize(ocs_lib):
     rc = L.ocs_batch_device_noalloc(ctypes.cast(reqs, ctypes.c_void_p), 1, None)
     torch.cuda.synchronize()
     assert rc == 0 and reqs[0].status == ocs_lib.OCS_EINVAL
+    # many distinct window tables at 2^13: more than the array's window
+    # region holds, so nothing is launched and every accepted request says so
+    n = 1 << 14
+    xs = torch.zeros(n, device="cuda")
+    g = ocs_lib.geometry(n, 13, 0.5, "--gaussian_window=x0.3<<sigma")
+    outs = [torch.zeros(g.out_floats, device="cuda") for _ in range(40)]
+    reqs = ocs_lib.make_requests([(xs, n, 13, 0.5, f"--gaussian_window=x0.{10 + i}<<sigma", outs[i], g.out_floats)
+                                  for i in range(40)])
+    rc = L.ocs_batch_device_noalloc(ctypes.cast(reqs, ctypes.c_void_p), len(reqs), None)
+    torch.cuda.synchronize()
+    assert rc == ocs_lib.OCS_ENOMEM and "window tables" in ocs_lib.last_error()
+    assert all(r.status == ocs_lib.OCS_ENOMEM for r in reqs)
+
+
+def test_noalloc_refuses_tensor_core_precision(ocs_lib):
+    """The tensor-core forms need tables the array has no room for: such a
+    request is refused with a status, never run in FP32 instead."""
+    import torch
+
+    L = ocs_lib.lib()
+    n = 1 << 14
+    x = torch.from_numpy(signal(71, n)).cuda()
+    opts = "--hanning_window --precision=tc-fp16"
+    g = ocs_lib.geometry(n, 10, 0.5, opts)
+    out = torch.full((g.out_floats,), float("nan"), device="cuda")
+    reqs = ocs_lib.make_requests([(x, n, 10, 0.5, opts, out, g.out_floats)])
+    rc = L.ocs_batch_device_noalloc(ctypes.cast(reqs, ctypes.c_void_p), 1, None)
+    torch.cuda.synchronize()
+    assert rc == 0 and reqs[0].status == ocs_lib.OCS_EINVAL
+    assert bool(torch.isnan(out).all())
+
+
+def test_noalloc_refused_under_stream_capture(ocs_lib):
+    """A call on a stream that is capturing a CUDA graph returns OCS_EINVAL
+    and launches nothing: its descriptors go through a host staging buffer
+    that every later call rewrites, so a replay could not reproduce it."""
+    import torch
+
+    L = ocs_lib.lib()
+    n = 1 << 14
+    x = torch.from_numpy(signal(72, n)).cuda()
+    g = ocs_lib.geometry(n, 9, 0.5, "--hamming_window")
+    out = torch.full((g.out_floats,), float("nan"), device="cuda")
+    reqs = ocs_lib.make_requests([(x, n, 9, 0.5, "--hamming_window", out, g.out_floats)])
+    # set-up (the first call on the device synchronizes its stream) before the capture
+    assert L.ocs_batch_device_noalloc(ctypes.cast(reqs, ctypes.c_void_p), 0, None) == 0
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        rc = L.ocs_batch_device_noalloc(ctypes.cast(reqs, ctypes.c_void_p), 1,
+                                        torch.cuda.current_stream().cuda_stream)
+    assert rc == ocs_lib.OCS_EINVAL and "graph" in ocs_lib.last_error()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert bool(torch.isnan(out).all())
+    # the same call outside the capture still works
+    rc = L.ocs_batch_device_noalloc(ctypes.cast(reqs, ctypes.c_void_p), 1, None)
+    torch.cuda.synchronize()
+    assert rc == 0 and reqs[0].status == 0 and not bool(torch.isnan(out).any())
