@@ -200,18 +200,41 @@ def dist_setup():
 
 
 # --------------------------------------------------------------- CPU legs
+# Samples per CPU step: the same bounded slice of the 1e8-sample signal in the
+# reference arm and in cpu_baseline, so that the two numbers describe one thing.
+CPU_SAMPLE = 1 << 22
+# Port at the reference's cost against the reference's own OpenMP build (-O3),
+# same 2^22-sample slice, measured on an 8-thread x86 host where both run:
+# the port evaluates windows per sample and twiddles per butterfly, as the
+# reference does, and runs 1.35x faster on 8 threads (0.91x on one).  The
+# table-driven port, without that cost model, ran 2.2-2.6x faster.
+PORT_VS_REFERENCE = "port at the reference's per-element cost: 1.35x the reference's own OpenMP build on 8 x86 " \
+                    "threads (0.91x on one), so the port understates the reference's time"
+
+
+def port_at_reference_cost(x: np.ndarray, nthreads: int) -> np.ndarray:
+    """The oracle port timed with the reference's per-element work (window per
+    sample, twiddle per butterfly); the oracle returns to its table form after."""
+    from oracle import orc
+
+    orc.set_reference_cost(True)
+    try:
+        return orc.serial_pipeline(x, HEAD_EXP, HEAD_OV, HEAD_OPTS, nthreads=nthreads)
+    finally:
+        orc.set_reference_cost(False)
+
+
 def cpu_reference_impl():
-    """The reference's OpenMP runner built from source if present, else the oracle port."""
+    """The reference's OpenMP runner built from source if present, else the oracle port at the reference's cost."""
     from oracle import orc
 
     if orc.RefLib.available("libref_openmp_fast.so"):
         R = orc.RefLib("libref_openmp_fast.so")
         return "reference", (lambda x: R.activate(x, HEAD_EXP, HEAD_OV, HEAD_OPTS)[0]), \
             "reference OpenMP runner (StandAlone/cross_gpgpu/OpenMP) built -O3 from source"
-    orc.lib()
     nt = os.cpu_count() or 1
-    return "port", (lambda x: orc.serial_pipeline(x, HEAD_EXP, HEAD_OV, HEAD_OPTS, nthreads=nt)), \
-        "oracle port of the reference OpenMP runner (bit-exact to it), OpenMP over all host cores"
+    return "port", (lambda x: port_at_reference_cost(x, nt)), \
+        "oracle port of the reference OpenMP runner (bit-exact to it), OpenMP over all host cores; " + PORT_VS_REFERENCE
 
 
 def cpu_serial_baseline(sample_n: int = 1 << 21, budget_s: float = 3.0) -> dict:
@@ -225,9 +248,8 @@ def cpu_serial_baseline(sample_n: int = 1 << 21, budget_s: float = 3.0) -> dict:
         kind, desc = "reference", "reference Serial runner (StandAlone/cross_gpgpu/Serial) built -O2 from source"
         fn = lambda x: R.activate(x, HEAD_EXP, HEAD_OV, HEAD_OPTS)[0]  # noqa: E731
     else:
-        orc.lib()
-        kind, desc = "port", "oracle port of the reference Serial runner (bit-exact to it)"
-        fn = lambda x: orc.serial_pipeline(x, HEAD_EXP, HEAD_OV, HEAD_OPTS, nthreads=1)  # noqa: E731
+        kind, desc = "port", "oracle port of the reference Serial runner (bit-exact to it); " + PORT_VS_REFERENCE
+        fn = lambda x: port_at_reference_cost(x, 1)  # noqa: E731
     x = make_signal_np(sample_n)
     fn(x)  # warm
     times = []
@@ -242,7 +264,7 @@ def cpu_serial_baseline(sample_n: int = 1 << 21, budget_s: float = 3.0) -> dict:
                       f"{desc}, one thread"}
 
 
-def cpu_baseline(sample_n: int = 1 << 23, budget_s: float = 12.0):
+def cpu_baseline(sample_n: int = CPU_SAMPLE, budget_s: float = 12.0):
     kind, fn, desc = cpu_reference_impl()
     x = make_signal_np(sample_n)
     fn(x)  # warm
@@ -264,7 +286,7 @@ def run_reference_arm(args):
     if rank != 0:
         return
     kind, fn, desc = cpu_reference_impl()
-    sample_n = 1 << 22
+    sample_n = CPU_SAMPLE
     x = make_signal_np(sample_n)
     for _ in range(args.warmup):
         fn(x)
@@ -279,7 +301,12 @@ def run_reference_arm(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "fused STFT, 1e8-sample multi-sinusoid signal, N=1024 Hamming, overlap 0.5, power "
                                "(reference layout); each step a bounded sample", "window": 1024, "overlap": 0.5,
-                   "output": "power", "sample_samples": sample_n},
+                   "output": "power", "sample_samples": sample_n,
+                   "sample_fraction": round(sample_n / 100_000_000, 4),
+                   "same_config": False,
+                   "note": f"each step runs the first {sample_n} samples ({sample_n / 1e6:.1f}%) of the 1e8-sample "
+                           "signal; the throughput per sample is comparable, and the small slice favours the CPU "
+                           "(its working set stays closer to the caches)"},
         "cpu_baseline": {"value": v, "unit": METRIC, "cores": os.cpu_count(), "kind": kind,
                          "sample": f"first {sample_n} samples per step; {desc}"},
         "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -603,10 +630,20 @@ def run_serving_leg(ocs, rates=(2000, 10000, 50000), durations=(1.0, 0.5, 0.3), 
 
 # ---------------------------------------------------------------- accuracy
 # FP64 reference for the accuracy slices, written with numpy (the oracle is
-# kept for the CPU baseline legs): the same framing, the library's window
-# table, a float64 real FFT, |X| in the reference layout (N bins per frame,
-# bins above N/2 mirrored).
-_WIN_KIND = {"--hanning_window": 1, "--hamming_window": 2, "--blackman_window": 3}
+# kept for the CPU baseline legs): the same framing, the window evaluated in
+# float64 from its formula (OKL/kernel.okl:33-56; independent of the library's
+# own table, which rounds like the reference's serial build), a float64 real
+# FFT, |X| in the reference layout (N bins per frame, bins above N/2 mirrored).
+def window_fp64(opts: str, N: int) -> np.ndarray:
+    i = np.arange(N, dtype=np.float64)
+    if "--hanning_window" in opts:
+        return 0.5 * (1.0 - np.cos(2 * np.pi * i / (N - 1)))
+    if "--hamming_window" in opts:
+        return 0.54 - 0.46 * np.cos(2 * np.pi * i / (N - 1))
+    if "--blackman_window" in opts:
+        a = 2 * np.pi * i / N
+        return 0.42 - 0.5 * np.cos(a) + 0.08 * np.cos(2 * a)
+    return np.ones(N)
 
 
 def geo_is_power_compat(opts: str) -> bool:
@@ -617,10 +654,9 @@ def geo_is_power_compat(opts: str) -> bool:
                                       "--flattop_window", "--gaussian_window"))
 
 
-def fp64_power_reference(ocs, xs: np.ndarray, exp: int, hop: int, nf: int, opts: str) -> np.ndarray:
+def fp64_power_reference(xs: np.ndarray, exp: int, hop: int, nf: int, opts: str) -> np.ndarray:
     N = 1 << exp
-    kind = next((k for o, k in _WIN_KIND.items() if o in opts), 0)
-    w = ocs.window_table(kind, N).astype(np.float64) if kind else np.ones(N)
+    w = window_fp64(opts, N)
     x = np.zeros((nf - 1) * hop + N)
     x[: xs.size] = xs[: x.size]
     frames = np.lib.stride_tricks.as_strided(x, shape=(nf, N), strides=(hop * 8, 8)) * w
@@ -669,7 +705,7 @@ def run_tc_leg(ocs, x, n, d_out, stream, steps=10, warmup=3):
             s0 = f0 * g.hop
             xs = x[s0:s0 + (nf - 1) * g.hop + g.n_window].cpu().numpy()
             got = d_out[f0 * g.n_window:(f0 + nf) * g.n_window].cpu().numpy()
-            ref = fp64_power_reference(ocs, xs, exp, g.hop, nf, "--hanning_window")
+            ref = fp64_power_reference(xs, exp, g.hop, nf, "--hanning_window")
             b = algorithmic_bytes(n, g, False, False)
             rows.append({"N": 1 << exp, "precision": prec, "gsamples_s": round(n / dt / 1e9, 2),
                          "ms": round(dt * 1e3, 4), "hbm_frac": round(b / dt / 1e9 / peak, 3),
@@ -683,12 +719,28 @@ def run_tc_leg(ocs, x, n, d_out, stream, steps=10, warmup=3):
                                       "numpy FFT of 300 frames"}
 
 
+def cpu_baseline_subprocess() -> dict:
+    """cpu_baseline in a fresh process started before this one initialises
+    CUDA: no GPU-side threads, pinned buffers or earlier legs share the host
+    cores with it, as none do in the reference arm's process."""
+    r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-leg", "--n", str(N_SAMPLES),
+                        "--exp", str(HEAD_EXP), "--overlap", str(HEAD_OV), "--options", HEAD_OPTS],
+                       capture_output=True, text=True, timeout=600)
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    if r.returncode != 0 or not lines:
+        return {"unavailable": f"CPU leg failed (rc {r.returncode}): {r.stderr.strip()[-300:]}"}
+    return json.loads(lines[-1])
+
+
 def run_ours(args):
+    ws, rank, local = dist_setup()
+    # the CPU baseline runs first, on rank 0 at N=1 only, before CUDA starts
+    cpu = cpu_baseline_subprocess() if (rank == 0 and ws == 1 and not args.no_cpu) else None
+
     import torch
 
     import occastft_gb300 as ocs
 
-    ws, rank, local = dist_setup()
     torch.cuda.set_device(local)
     if ws > 1:
         import torch.distributed as dist
@@ -755,7 +807,7 @@ def run_ours(args):
         if not geo_is_power_compat(HEAD_OPTS):
             acc = {"skipped": "float64 check covers power in the reference layout"}
         else:
-            ref = fp64_power_reference(ocs, xs, HEAD_EXP, geo.hop, nf, HEAD_OPTS)
+            ref = fp64_power_reference(xs, HEAD_EXP, geo.hop, nf, HEAD_OPTS)
             acc = {"rel_l2_vs_fp64": rel_l2(got, ref), "max_db_vs_fp64": max_db_error(got, ref),
                    "frames_checked": nf}
 
@@ -859,10 +911,9 @@ def run_ours(args):
             dist.destroy_process_group()
         return
 
-    cpu = None if args.no_cpu else cpu_baseline()
     headline = (n == 100_000_000 and HEAD_EXP == 10 and HEAD_OV == 0.5 and HEAD_OPTS == "--hamming_window")
     # the committed ncu traffic figure belongs to the headline workload only
-    traffic = load_traffic(f"stft_fused_e{HEAD_EXP}_hamming_power_1e8") if headline else None
+    traffic = load_traffic(f"stft_pair_e{HEAD_EXP}_hamming_power_1e8") if headline else None
     if headline:
         workload = ("fused STFT of a 1e8-sample float32 signal (8 seeded sinusoids + N(0,0.01^2), fs 48 kHz), "
                     "window 1024 Hamming, overlap 0.5, power in the reference layout (qt x N floats)")
@@ -915,11 +966,14 @@ def main():
     ap.add_argument("--exp", type=int, default=HEAD_EXP)
     ap.add_argument("--options", default=HEAD_OPTS)
     ap.add_argument("--overlap", type=float, default=HEAD_OV)
+    ap.add_argument("--cpu-leg", action="store_true", help=argparse.SUPPRESS)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     globals().update(N_SAMPLES=args.n, HEAD_EXP=args.exp, HEAD_OPTS=args.options, HEAD_OV=args.overlap)
-    if args.impl == "reference":
+    if args.cpu_leg:
+        print(json.dumps(cpu_baseline()))
+    elif args.impl == "reference":
         run_reference_arm(args)
     else:
         run_ours(args)

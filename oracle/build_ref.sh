@@ -11,9 +11,12 @@
 # (types, toQuot and the runnerFunction declarations, without the server
 # includes), and Default_Pipeline is taken from lines 166-318 of
 # GLOBAL/RunnerCommon.cpp.  No reference source is written into the repo.
+#
+# The reference checkout is taken from $OCS_REFERENCE, else from a directory
+# named "reference" beside this repository's root.
 set -euo pipefail
-REF=${OCS_REFERENCE:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${OCS_REFERENCE:-$(cd "$HERE/../.." && pwd)/reference}
 OUT="$HERE/_ref"
 G="$REF/StandAlone/cross_gpgpu"
 if [ ! -d "$G/GLOBAL" ]; then

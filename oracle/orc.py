@@ -83,6 +83,7 @@ def lib() -> ctypes.CDLL:
         L.orc_apply_window.argtypes = [ctypes.c_int, fp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float,
                                        ctypes.c_int]
         L.orc_remove_dc.argtypes = [fp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int]
+        L.orc_set_reference_cost.argtypes = [ctypes.c_int]
         _lib = L
     return _lib
 
@@ -129,6 +130,12 @@ def serial_pipeline(x: np.ndarray, exp: int, overlap: float, options: str, fix_p
     if rc != 0:
         raise ValueError(f"oracle pipeline failed rc={rc}")
     return out
+
+
+def set_reference_cost(on: bool) -> None:
+    """Time the port at the reference's cost: window coefficients evaluated per
+    sample and twiddles per butterfly (the outputs do not change)."""
+    lib().orc_set_reference_cost(1 if on else 0)
 
 
 def fp64_stft(x: np.ndarray, exp: int, overlap: float, options: str, nthreads: int = 0) -> np.ndarray:

@@ -208,10 +208,27 @@ void orc_overlap(const float* in, uint32_t ofull, uint32_t n, uint32_t exp, uint
     }
 }
 
+/* Cost model of the timed CPU baseline.  0 (default): tables built once per
+ * call, the fast form for checking.  1: the reference's own per-element work
+ * (a window coefficient evaluated for every sample, as Window_* does, and
+ * cos/sin of the twiddle angle for every butterfly, as kernel.okl:146-153
+ * does), so that the port's time is the reference's time.  The values, and so
+ * the outputs, are the same in both modes: each is the same float expression. */
+static int g_reference_cost = 0;
+
+void orc_set_reference_cost(int on) { g_reference_cost = on ? 1 : 0; }
+
 /* EXPCommon.okl:29-148 */
 void orc_apply_window(int kind, float* data, uint32_t ofull, uint32_t nwin, float sigma, int nthreads)
 {
     if (kind == ORC_WIN_NONE) return;
+    if (g_reference_cost) {
+        const int64_t total = ofull;
+#pragma omp parallel for num_threads(nthreads) schedule(static) if (nthreads > 1)
+        for (int64_t i = 0; i < total; ++i)
+            data[i] *= orc_window_value(kind, (int)((uint64_t)i & (nwin - 1)), (int)nwin, sigma);
+        return;
+    }
     float* w = (float*)malloc(sizeof(float) * nwin);
     for (uint32_t i = 0; i < nwin; ++i) w[i] = orc_window_value(kind, (int)i, (int)nwin, sigma);
     const int64_t frames = ofull / nwin;
@@ -266,6 +283,32 @@ static void orc_stockham_stage(const float* inR, const float* inI, float* outR, 
         twi[r] = sinf(ang);
     }
     const int64_t frames = ohalf / h;
+    if (g_reference_cost) {
+        /* the twiddle of every butterfly evaluated where it is used */
+#pragma omp parallel for num_threads(nthreads) schedule(static) if (nthreads > 1)
+        for (int64_t gi = 0; gi < frames; ++gi) {
+            const uint64_t base = (uint64_t)gi * n2;
+            for (uint32_t gx = 0; gx < h; ++gx) {
+                const uint64_t o = base + gx;
+                const float lr = inR[o], li = inI[o];
+                const float rr = inR[o + h], ri = inI[o + h];
+                const uint64_t ls = (uint64_t)(gx >> stage) * (seg << 1) + (gx & (seg - 1)) + base;
+                const uint64_t rs = ls + seg;
+                const int k = (int)(((int)(gx & (seg - 1)) * (int)h) / (int)seg);
+                const float ang = (float)(-2.0 * ORC_PI * (double)((float)k / (float)n2));
+                const float tr = cosf(ang), ti = sinf(ang);
+                const float rt = rr * tr - ri * ti;
+                const float it = rr * ti + ri * tr;
+                outR[ls] = lr + rt;
+                outI[ls] = li + it;
+                outR[rs] = lr - rt;
+                outI[rs] = li - it;
+            }
+        }
+        free(twr);
+        free(twi);
+        return;
+    }
 #pragma omp parallel for num_threads(nthreads) schedule(static) if (nthreads > 1)
     for (int64_t gi = 0; gi < frames; ++gi) {
         const uint64_t base = (uint64_t)gi * n2;

@@ -64,6 +64,10 @@ int orc_serial_pipeline(const float* in, uint32_t n, int exp, float overlap,
 uint64_t orc_output_floats(const orc_geometry* g, const orc_options* o);
 int orc_fp64_stft(const float* in, uint32_t n, int exp, float overlap,
                   const char* options, double* out, uint64_t out_cap, int nthreads);
+/* 1: evaluate window coefficients per sample and twiddles per butterfly, as
+ * the reference does (same values; used to time the CPU baseline at the
+ * reference's cost); 0: per-call tables (default) */
+void orc_set_reference_cost(int on);
 /* per-stage restatements (float32) */
 void orc_overlap(const float* in, uint32_t ofull, uint32_t n, uint32_t exp, uint32_t hop, float* real);
 void orc_apply_window(int kind, float* data, uint32_t ofull, uint32_t n_window, float sigma, int nthreads);

@@ -2,6 +2,8 @@
 roofline fraction and the FP32-pipe bound reported beside it."""
 import math
 
+import numpy as np
+
 import pytest
 
 import bench
@@ -90,3 +92,24 @@ def test_reference_arm_other_ranks_exit_quietly():
     r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--steps", "1"],
                        capture_output=True, text=True, timeout=300, cwd=root, env=env)
     assert r.returncode == 0 and "{" not in r.stdout, r.stdout + r.stderr[-2000:]
+
+
+@pytest.mark.parametrize("opts", ["--hanning_window", "--hamming_window", "--blackman_window"])
+def test_accuracy_window_is_independent_and_agrees(orc, opts):
+    """The bench's accuracy check evaluates its window in float64 from the
+    formula, not from the library's table; the two agree to float rounding."""
+    N = 1024
+    kind = opts[2:].split("_")[0]
+    ref = orc.window(kind, N).astype(np.float64)
+    w = bench.window_fp64(opts, N)
+    assert np.max(np.abs(w - ref)) <= 2e-7
+
+
+def test_cpu_baseline_uses_the_reference_arms_sample():
+    """cpu_baseline and the reference arm time the same slice of the signal."""
+    import inspect
+
+    assert inspect.signature(bench.cpu_baseline).parameters["sample_n"].default == bench.CPU_SAMPLE
+    r = bench.cpu_baseline(sample_n=1 << 16, budget_s=0.2)
+    assert r["value"] > 0 and r["kind"] in ("reference", "port") and r["cores"] >= 1
+    assert r["serial_1core"]["cores"] == 1

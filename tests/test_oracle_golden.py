@@ -85,3 +85,18 @@ def test_p4_quirk_reproduced_and_fixed(orc, golden):
         f64 = orc.fp64_stft(x, c["exp"], c["overlap"], c["options"] + " --serial_power")
         assert orc.rel_l2(fixed, f64) < 1e-5
         assert orc.rel_l2(arrays[c["name"]], f64) > 0.1
+
+
+def test_reference_cost_model_changes_no_output(orc):
+    """The port's two cost models (per-call tables; per-element trig as the
+    reference computes it) give the same bits."""
+    x = signal(8, 40000)
+    for exp, op in ((6, "--hanning_window --remove_dc"), (10, "--hamming_window"),
+                    (13, "--nuttall_window --half_complex_return"), (9, "--gaussian_window=x0.4<<sigma")):
+        a = orc.serial_pipeline(x, exp, 0.5, op, nthreads=2)
+        orc.set_reference_cost(True)
+        try:
+            b = orc.serial_pipeline(x, exp, 0.5, op, nthreads=2)
+        finally:
+            orc.set_reference_cost(False)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (exp, op)

@@ -36,3 +36,20 @@ def test_openmp_equals_serial(orc):
         a, _ = S.activate(x, exp, 0.5, "--hanning_window --remove_dc")
         b, _ = O.activate(x, exp, 0.5, "--hanning_window --remove_dc")
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+@ref_missing
+def test_port_at_reference_cost_matches_reference(orc):
+    """The cost model the CPU baseline is timed with (window per sample,
+    twiddle per butterfly) gives the reference's output bit for bit."""
+    O = orc.RefLib("libref_openmp.so")
+    x = signal(4, 70000)
+    orc.set_reference_cost(True)
+    try:
+        for exp, op in ((10, "--hamming_window"), (12, "--blackman_window --remove_dc"),
+                        (7, "--hanning_window --half_complex_return")):
+            ref, _ = O.activate(x, exp, 0.5, op)
+            mine = orc.serial_pipeline(x, exp, 0.5, op, nthreads=4)
+            assert np.array_equal(ref.view(np.uint32), mine.view(np.uint32)), (exp, op)
+    finally:
+        orc.set_reference_cost(False)
