@@ -24,7 +24,7 @@ STANDALONE = os.path.join(PKG, "standalone")
 CUDARUN = os.path.join(PKG, "cudaRun")
 STANDALONE_SOURCES = ["request_codec.cpp", "ws_server.cpp", "shm_payload.cpp", "cudaRun.cpp"]
 
-CU_SOURCES = ["stft_fused.cu", "stft_fused_lo.cu", "stft_fused_hi.cu", "stft_pair_lo.cu", "stft_pair_hi.cu",
+CU_SOURCES = ["stft_fused.cu", "stft_fused_lo.cu", "stft_fused_hi.cu", "stft_pair_lo.cu", "stft_pair_hi.cu", "stft_pairx2.cu",
               "stft_batch.cu", "stft_batch_noalloc.cu", "stft_tc.cu", "stft_stages.cu", "stft_large.cu", "stft_tpf.cu"]
 CPP_SOURCES = ["ocs_api.cpp", "ocs_host.cpp", "ocs_server.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

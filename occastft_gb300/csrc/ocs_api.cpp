@@ -223,8 +223,9 @@ const float* host_window(const float* d)
 // Variants of the fused kernel: 0 one frame per FFT, direct I/O; 1 one frame
 // per FFT, shared-memory staged I/O (windows <= 2^9); 2 two frames per FFT;
 // 3 N/64 lanes per frame, the FFT in registers (windows 2^6 .. 2^8 for power,
-// 2^6 for half-complex).
-enum { VAR_DIRECT = 0, VAR_STAGED = 1, VAR_PAIR = 2, VAR_TPF = 3, VAR_COUNT = 4 };
+// 2^6 for half-complex); 4 two frames per FFT on packed FP32x2 arithmetic
+// (window 2^10).
+enum { VAR_DIRECT = 0, VAR_STAGED = 1, VAR_PAIR = 2, VAR_TPF = 3, VAR_PAIRX2 = 4, VAR_COUNT = 5 };
 
 bool env_is(const char* name, const char* val)
 {
@@ -239,7 +240,8 @@ int default_variant(int exp, int outk)
     const bool power = outk != ocs::OUT_HALF;
     if (power) {
         if (exp <= 8) return VAR_TPF;
-        if (exp == 9 || exp == 10 || exp == 12 || exp == 13 || exp == 14) return VAR_PAIR;
+        if (exp == 10) return VAR_PAIRX2;
+        if (exp == 9 || exp == 12 || exp == 13 || exp == 14) return VAR_PAIR;
         return VAR_DIRECT;
     }
     if (exp == 6) return VAR_TPF;
@@ -248,6 +250,8 @@ int default_variant(int exp, int outk)
 }
 bool variant_ok(int v, int exp, int outk, bool out16)
 {
+    if (v == VAR_PAIRX2)
+        return ocs::pairx2_has(exp, outk) && !env_is("OCS_KERNEL", "single") && !env_is("OCS_KERNEL", "pair");
     if (v == VAR_PAIR) return ocs::pair_has(exp) && outk != ocs::OUT_PLANES && !env_is("OCS_KERNEL", "single");
     if (v == VAR_STAGED)
         return ocs::fused_has_staged(exp) && outk != ocs::OUT_PLANES && out16 && !env_is("OCS_IO_SCHEME", "direct");
@@ -302,17 +306,19 @@ int grid_size(int exp, int outk, int variant, uint64_t frames)
         auto key = std::make_pair(exp, outk * 4 + variant);
         auto it = c.occupancy.find(key);
         if (it == c.occupancy.end()) {
-            occ = std::max(1, variant == VAR_PAIR  ? ocs::pair_occupancy(exp, outk)
-                              : variant == VAR_TPF ? ocs::tpf_occupancy(exp, outk)
-                                                   : ocs::fused_occupancy(exp, outk, variant == VAR_STAGED));
+            occ = std::max(1, variant == VAR_PAIR     ? ocs::pair_occupancy(exp, outk)
+                              : variant == VAR_PAIRX2 ? ocs::pairx2_occupancy(exp, outk)
+                              : variant == VAR_TPF    ? ocs::tpf_occupancy(exp, outk)
+                                                      : ocs::fused_occupancy(exp, outk, variant == VAR_STAGED));
             c.occupancy[key] = occ;
         } else {
             occ = it->second;
         }
     }
-    const uint64_t fpc = (uint64_t)(variant == VAR_PAIR  ? 2 * ocs::pair_per_cta(exp)
-                                    : variant == VAR_TPF ? ocs::tpf_frames_per_cta(exp)
-                                                         : ocs::fused_frames_per_cta(exp));
+    const uint64_t fpc = (uint64_t)(variant == VAR_PAIR     ? 2 * ocs::pair_per_cta(exp)
+                                    : variant == VAR_PAIRX2 ? 2 * ocs::pairx2_per_cta(exp)
+                                    : variant == VAR_TPF    ? ocs::tpf_frames_per_cta(exp)
+                                                            : ocs::fused_frames_per_cta(exp));
     const uint64_t need = (frames + fpc - 1) / fpc;
     const uint64_t full = (uint64_t)c.sms * occ;
     return (int)std::max<uint64_t>(1, std::min(need, full));
@@ -346,6 +352,10 @@ cudaError_t launch_variant(int v, const Request& r, int outk, ocs::FusedArgs a, 
     if (v == VAR_PAIR) {
         a.tw = tw_pair;
         return ocs::launch_pair(r.exp, outk, a, grid_size(r.exp, outk, VAR_PAIR, a.frames), st);
+    }
+    if (v == VAR_PAIRX2) {
+        a.tw = tw_pair;
+        return ocs::launch_pairx2(r.exp, outk, a, grid_size(r.exp, outk, VAR_PAIRX2, a.frames), st);
     }
     if (v == VAR_TPF) {
         const float* hw = host_window(a.win);
@@ -505,6 +515,14 @@ int launch_frames(const Request& r, const float* d_sig, uint64_t n, float* d_out
         if (variant_ok(v, r.exp, outk, out16)) cand[nc++] = v;
     if (env_is("OCS_KERNEL", "tpf") && variant_ok(VAR_TPF, r.exp, outk, out16)) {
         OCS_CUDA(launch_variant(VAR_TPF, r, outk, a, tw_single, tw_pair, st));
+        return OCS_OK;
+    }
+    if (env_is("OCS_KERNEL", "x2") && variant_ok(VAR_PAIRX2, r.exp, outk, out16)) {
+        OCS_CUDA(launch_variant(VAR_PAIRX2, r, outk, a, tw_single, tw_pair, st));
+        return OCS_OK;
+    }
+    if (env_is("OCS_KERNEL", "pair") && variant_ok(VAR_PAIR, r.exp, outk, out16)) {
+        OCS_CUDA(launch_variant(VAR_PAIR, r, outk, a, tw_single, tw_pair, st));
         return OCS_OK;
     }
     int choice = default_variant(r.exp, outk);

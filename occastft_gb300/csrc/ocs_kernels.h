@@ -70,6 +70,13 @@ int pair_per_cta(int exp);
 int pair_twiddle_count(int exp);
 cudaError_t build_pair_twiddles(float2* tw, int exp, cudaStream_t st);
 
+// paired-frame STFT on packed FP32x2 arithmetic (window 2^10): same plan
+// table (a.tw = the pair plan's), one warp per frame pair, 8 pairs per CTA
+bool pairx2_has(int exp, int outk);
+cudaError_t launch_pairx2(int exp, int outk, const FusedArgs& a, int grid, cudaStream_t st);
+int pairx2_occupancy(int exp, int outk);
+int pairx2_per_cta(int exp);
+
 // uneven batch: one persistent launch over a device tile queue
 struct BatchTile {
     uint32_t req;      // index into the request descriptors

@@ -115,6 +115,14 @@ cudaError_t launch_large(int exp, int outk, const LargeArgs& a, uint64_t frames,
     return cudaSuccess;
 }
 
+bool pairx2_has(int exp, int outk) { return exp == 10 && outk != OUT_PLANES; }
+cudaError_t launch_pairx2(int exp, int outk, const FusedArgs& a, int, cudaStream_t st)
+{
+    return fused_like(exp, outk, a, st);
+}
+int pairx2_occupancy(int, int) { return 2; }
+int pairx2_per_cta(int) { return 8; }
+
 bool tc_supports(int exp) { return exp >= 8 && exp <= 12; }
 bool tc_mode_supported(int exp, int pm) { return !(exp == 12 && pm == 3); }
 bool tc_piped(int exp, uint64_t hop) { return (exp != 8 && exp != 10) || hop <= (1ull << exp); }

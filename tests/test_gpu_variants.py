@@ -1,5 +1,6 @@
 """Every kernel variant (one frame per FFT with direct or staged I/O, two
-frames per FFT) against the FP64 oracle.  Variants are forced through the
+frames per FFT in scalar or packed FP32x2 arithmetic, lanes per frame)
+against the FP64 oracle.  Variants are forced through the
 runner's environment switches in a child process, so each one is exercised
 regardless of which the autotuner would pick."""
 import json
@@ -35,6 +36,8 @@ print(json.dumps(res))
 
 @pytest.mark.parametrize("env", [
     {"OCS_KERNEL": "tpf", "OCS_AUTOTUNE": "0"},
+    {"OCS_KERNEL": "x2", "OCS_AUTOTUNE": "0"},
+    {"OCS_KERNEL": "pair", "OCS_AUTOTUNE": "0"},
     {"OCS_KERNEL": "single", "OCS_IO_SCHEME": "direct", "OCS_AUTOTUNE": "0"},
     {"OCS_KERNEL": "single", "OCS_AUTOTUNE": "0"},
     {"OCS_AUTOTUNE": "0"},
