@@ -724,7 +724,7 @@ def cpu_baseline_subprocess() -> dict:
     CUDA: no GPU-side threads, pinned buffers or earlier legs share the host
     cores with it, as none do in the reference arm's process."""
     r = subprocess.run([sys.executable, os.path.abspath(__file__), "--cpu-leg", "--n", str(N_SAMPLES),
-                        "--exp", str(HEAD_EXP), "--overlap", str(HEAD_OV), "--options", HEAD_OPTS],
+                        "--exp", str(HEAD_EXP), "--overlap", str(HEAD_OV), "--options=" + HEAD_OPTS],
                        capture_output=True, text=True, timeout=600)
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
     if r.returncode != 0 or not lines:
@@ -967,12 +967,16 @@ def main():
     ap.add_argument("--options", default=HEAD_OPTS)
     ap.add_argument("--overlap", type=float, default=HEAD_OV)
     ap.add_argument("--cpu-leg", action="store_true", help=argparse.SUPPRESS)
+    ap.add_argument("--cpu-sample", type=int, default=0, help=argparse.SUPPRESS)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     globals().update(N_SAMPLES=args.n, HEAD_EXP=args.exp, HEAD_OPTS=args.options, HEAD_OV=args.overlap)
     if args.cpu_leg:
-        print(json.dumps(cpu_baseline()))
+        if args.cpu_sample:
+            print(json.dumps(cpu_baseline(sample_n=args.cpu_sample, budget_s=0.5)))
+        else:
+            print(json.dumps(cpu_baseline()))
     elif args.impl == "reference":
         run_reference_arm(args)
     else:

@@ -86,8 +86,14 @@ __device__ __forceinline__ void batch_tile(const FusedArgs& a, uint64_t f0, uint
             b.tw = a.tw_pair;
             const int lp = tid / T, t = tid - lp * T;
             const TwTwoLevel tw2{nullptr, nullptr};
-            for (uint64_t pbase = f0 / 2; 2 * pbase < f0 + nf; pbase += PPC)
+            for (uint64_t pbase = f0 / 2; 2 * pbase < f0 + nf; pbase += PPC) {
+                const uint64_t q = pbase + PPC + lp;  // this group's next pair in the tile
+                if (t == 0 && 2 * q < b.frames) {
+                    const uint64_t s0 = 2 * q * b.hop, end = s0 + b.hop + (uint64_t)(1 << EXP);
+                    prefetch_l2_span(b.x, s0, end < b.n ? end : b.n);
+                }
                 pair_group<EXP, OUT_POWER>(b, pbase, smem + lp * BS, smem + PPC * BS, st, tw2, sw, tid, lp, t);
+            }
             return;
         }
     }
@@ -130,14 +136,19 @@ __device__ __forceinline__ void batch_tile(const FusedArgs& a, uint64_t f0, uint
     // specialised for it, except at 2^11 and 2^13, where the extra body makes
     // the kernel spill under its 128-register cap (2^11 tiles fell from 0.49
     // to 0.31 of HBM); other kinds take the run-time body.
+    // each frame group prefetches its next frame of the tile into L2
     auto run = [&](const auto& twx) {
         if (EXP != 11 && EXP != 13 && a.outk == OUT_POWER) {
-            for (uint64_t fb = f0; fb < f0 + nf; fb += FPC)
+            for (uint64_t fb = f0; fb < f0 + nf; fb += FPC) {
+                fused_prefetch_next<EXP>(b, fb + FPC + lf, t);
                 fused_group_frames<EXP, (EXP != 11 && EXP != 13) ? OUT_POWER : OUT_RUNTIME>(b, fb, buf, red, twx,
                                                                                              win2, tid, lf, t);
+            }
         } else {
-            for (uint64_t fb = f0; fb < f0 + nf; fb += FPC)
+            for (uint64_t fb = f0; fb < f0 + nf; fb += FPC) {
+                fused_prefetch_next<EXP>(b, fb + FPC + lf, t);
                 fused_group_frames<EXP, OUT_RUNTIME>(b, fb, buf, red, twx, win2, tid, lf, t);
+            }
         }
     };
     if constexpr (EXP > kBatchSmemTabMaxExp) {
@@ -165,17 +176,30 @@ stft_batch_kernel(const FusedArgs* __restrict__ reqs, const BatchTile* __restric
     __shared__ uint32_t s_tile;
     __shared__ const float2* s_tw;  // tables now in shared memory (see batch_tile)
     __shared__ const float* s_win;
+    const uint32_t nt = *ntiles;
     if (threadIdx.x == 0) {
         s_tw = nullptr;
         s_win = nullptr;
+        s_tile = atomicAdd(counter, 1u);
     }
-    const uint32_t nt = *ntiles;
     for (;;) {
-        if (threadIdx.x == 0) s_tile = atomicAdd(counter, 1u);
-        __syncthreads();
+        __syncthreads();  // s_tile is written; the previous tile's smem use is over
         const uint32_t ti = s_tile;
-        __syncthreads();  // every thread has read s_tile; the previous tile's smem use is over
+        __syncthreads();  // every thread has read s_tile
         if (ti >= nt) break;
+        if (threadIdx.x == 0) {
+            // claim the next tile now and start its first frames toward L2,
+            // so that they arrive while this tile computes
+            const uint32_t nx = atomicAdd(counter, 1u);
+            s_tile = nx;
+            if (nx < nt) {
+                const BatchTile tn = tiles[nx];
+                const FusedArgs& an = reqs[tn.req];
+                const uint64_t k = tn.nframes < 16u ? tn.nframes : 16u;
+                const uint64_t s0 = tn.f0 * an.hop, end = (tn.f0 + k - 1) * an.hop + (1ull << an.exp);
+                prefetch_l2_span(an.x, s0, end < an.n ? end : an.n);
+            }
+        }
         const BatchTile tl = tiles[ti];
         const FusedArgs a = reqs[tl.req];
         switch (a.exp) {

@@ -96,6 +96,19 @@ __device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// Starts an L2 fill of samples [s0, s1) of x: the 16-byte-aligned interior of
+// the span as one bulk prefetch (a hint on this GPU's own memory; it holds no
+// registers or shared memory and completes on its own).  The persistent
+// kernels issue it for a frame (or pair) of their next iteration, so that the
+// loads of that iteration hit L2 instead of waiting on DRAM.
+__device__ __forceinline__ void prefetch_l2_span(const float* x, uint64_t s0, uint64_t s1)
+{
+    const uintptr_t b = (reinterpret_cast<uintptr_t>(x + s0) + 15) & ~(uintptr_t)15;
+    const uintptr_t e = reinterpret_cast<uintptr_t>(x + s1) & ~(uintptr_t)15;
+    if (s0 < s1 && b < e)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(b), "r"((unsigned)(e - b)) : "memory");
+}
+
 // ------------------------------------------------------------ plan constants
 // tables live in shared memory up to this exponent
 __host__ __device__ constexpr bool fused_tables_in_smem(int exp) { return exp <= 12; }
@@ -433,6 +446,18 @@ __device__ __forceinline__ void fused_group_frames(const FusedArgs& a, uint64_t 
     });
 }
 
+// L2 prefetch of frame f (the frame this thread's group takes next), issued
+// by the group's first thread
+template <int EXP>
+__device__ __forceinline__ void fused_prefetch_next(const FusedArgs& a, uint64_t f, int t)
+{
+    if (t == 0 && f < a.frames) {
+        const uint64_t s0 = f * a.hop;
+        const uint64_t s1 = s0 + (uint64_t)(1 << EXP) < a.n ? s0 + (uint64_t)(1 << EXP) : a.n;
+        prefetch_l2_span(a.x, s0, s1);
+    }
+}
+
 // CTAs per SM the register budget is sized for: three at window 2^13 (one
 // frame of 256 threads, 80 registers; measured 355 -> 403 Gsamples/s for
 // half-complex at 1e8 samples), otherwise two 256-thread CTAs or one larger
@@ -461,14 +486,18 @@ stft_fused_kernel(const FusedArgs a)
         const float2* tw;
         const float2* win2;
         load_tables<EXP>(a, s_tab, tid, tw, win2);
-        for (uint64_t fbase = (uint64_t)blockIdx.x * FPC; fbase < a.frames; fbase += (uint64_t)gridDim.x * FPC)
+        for (uint64_t fbase = (uint64_t)blockIdx.x * FPC; fbase < a.frames; fbase += (uint64_t)gridDim.x * FPC) {
+            fused_prefetch_next<EXP>(a, fbase + (uint64_t)gridDim.x * FPC + lf, t);
             fused_group_frames<EXP, OUTK>(a, fbase, buf, red, tw, win2, tid, lf, t);
+        }
     } else {
         const TwTwoLevel tw = build_tw2<EXP>(a.tw, s_tab, tid, blockDim.x);
         __syncthreads();
         const float2* win2 = reinterpret_cast<const float2*>(a.win);
-        for (uint64_t fbase = (uint64_t)blockIdx.x * FPC; fbase < a.frames; fbase += (uint64_t)gridDim.x * FPC)
+        for (uint64_t fbase = (uint64_t)blockIdx.x * FPC; fbase < a.frames; fbase += (uint64_t)gridDim.x * FPC) {
+            fused_prefetch_next<EXP>(a, fbase + (uint64_t)gridDim.x * FPC + lf, t);
             fused_group_frames<EXP, OUTK>(a, fbase, buf, red, tw, win2, tid, lf, t);
+        }
     }
 }
 

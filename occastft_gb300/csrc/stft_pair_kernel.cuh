@@ -293,8 +293,16 @@ stft_pair_kernel(const FusedArgs a)
     pair_tables<EXP>(a, s_tab, tid, win, tw2);
 
     const uint64_t pairs = (a.frames + 1) / 2;
-    for (uint64_t pbase = (uint64_t)blockIdx.x * PPC; pbase < pairs; pbase += (uint64_t)gridDim.x * PPC)
+    for (uint64_t pbase = (uint64_t)blockIdx.x * PPC; pbase < pairs; pbase += (uint64_t)gridDim.x * PPC) {
+        // L2 prefetch of the pair this group takes next: samples of frames 2q and 2q + 1
+        const uint64_t q = pbase + (uint64_t)gridDim.x * PPC + lp;
+        if (t == 0 && q < pairs) {
+            const uint64_t s0 = 2 * q * a.hop;
+            const uint64_t end = s0 + a.hop + (uint64_t)(1 << EXP);
+            prefetch_l2_span(a.x, s0, end < a.n ? end : a.n);
+        }
         pair_group<EXP, OUTK>(a, pbase, buf, red, s_tab, tw2, win, tid, lp, t);
+    }
 }
 
 // One CTA iteration: pairs pbase .. pbase + PPC - 1 (frames 2p, 2p + 1 below

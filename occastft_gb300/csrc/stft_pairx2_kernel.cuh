@@ -160,11 +160,7 @@ __global__ void __launch_bounds__(256, 2) stft_pairx2_kernel(const FusedArgs a)
         // bulk prefetch: no shared memory or registers held)
         if (t == 0 && p + stride < pairs) {
             const uint64_t s0 = 2 * (p + stride) * a.hop;
-            const uint64_t s1 = s0 + a.hop + N < a.n ? s0 + a.hop + N : a.n;
-            const uintptr_t b = (reinterpret_cast<uintptr_t>(a.x + s0) + 15) & ~(uintptr_t)15;
-            const uintptr_t e = reinterpret_cast<uintptr_t>(a.x + s1) & ~(uintptr_t)15;
-            if (s0 < s1 && b < e)
-                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(b), "r"((unsigned)(e - b)) : "memory");
+            prefetch_l2_span(a.x, s0, s0 + a.hop + N < a.n ? s0 + a.hop + N : a.n);
         }
         const uint64_t fa = 2 * p, fb = fa + 1;
         const bool act_b = fb < a.frames;  // frame a is always active here

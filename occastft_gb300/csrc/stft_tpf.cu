@@ -119,6 +119,17 @@ __device__ __forceinline__ void tpf_half_out(const FusedArgs& a, const float2 (&
     });
 }
 
+// L2 prefetch of the sample span of frames [f0, f0 + nf) (a warp's next
+// group), issued by lane 0
+__device__ __forceinline__ void tpf_prefetch_group(const FusedArgs& a, uint64_t f0, int nf, int N, int lane)
+{
+    if (lane == 0 && f0 < a.frames) {
+        const uint64_t last = f0 + (uint64_t)nf - 1 < a.frames ? f0 + (uint64_t)nf - 1 : a.frames - 1;
+        const uint64_t s0 = f0 * a.hop, s1 = last * a.hop + (uint64_t)N;
+        prefetch_l2_span(a.x, s0, s1 < a.n ? s1 : a.n);
+    }
+}
+
 template <int EXP, int OUTK>
 __global__ void __launch_bounds__(kTpfThreads, 2) stft_tpf_kernel(const FusedArgs a, const WinParam<1 << EXP> wp)
 {
@@ -135,6 +146,7 @@ __global__ void __launch_bounds__(kTpfThreads, 2) stft_tpf_kernel(const FusedArg
     const uint64_t wstride = (uint64_t)gridDim.x * (kTpfThreads / 32);
     for (uint64_t g = (uint64_t)blockIdx.x * (kTpfThreads / 32) + warp; g * 32 < a.frames; g += wstride) {
         const uint64_t f0 = g * 32;
+        tpf_prefetch_group(a, (g + wstride) * 32, 32, N, lane);
         // ---------------- 32 frames -> 32 rows
         const bool full = f0 + 32 <= a.frames && (f0 + 31) * a.hop + N <= a.n;
         if (cs == 16 && full) {

@@ -113,3 +113,22 @@ def test_cpu_baseline_uses_the_reference_arms_sample():
     r = bench.cpu_baseline(sample_n=1 << 16, budget_s=0.2)
     assert r["value"] > 0 and r["kind"] in ("reference", "port") and r["cores"] >= 1
     assert r["serial_1core"]["cores"] == 1
+
+
+def test_cpu_leg_subprocess_prints_its_line(monkeypatch):
+    """The CPU baseline runs as `bench.py --cpu-leg` in a fresh process; the
+    options string (which starts with "--") reaches it intact."""
+    monkeypatch.setattr(bench, "CPU_SAMPLE", 1 << 16)
+    import subprocess
+    import sys
+
+    real = subprocess.run
+
+    def small(cmd, **kw):
+        # the child times a small sample so that the test stays short
+        return real(cmd + ["--cpu-sample", str(1 << 16)], **kw) if "--cpu-leg" in cmd else real(cmd, **kw)
+
+    monkeypatch.setattr(subprocess, "run", small)
+    r = bench.cpu_baseline_subprocess()
+    assert "unavailable" not in r, r
+    assert r["value"] > 0 and r["kind"] in ("reference", "port") and r["serial_1core"]["cores"] == 1
