@@ -401,30 +401,47 @@ __device__ __forceinline__ void fused_group_frames(const FusedArgs& a, uint64_t 
     const int src = K::partner_lane(tid, t);
 
     // ---------------- untangle + fused output store
-    static_for<0, R>([&](auto uc) {
+    // Power and planes: one untangle at bin k < M/2 gives X[k] and X[k + M],
+    // and with them, for a real frame, X[N - k] = conj X[k] and
+    // X[M - k] = conj X[M + k], so slots u < R/2 (k = t + u T < M/2) cover
+    // every bin and slot R/2 of the group's first thread adds k = M/2.
+    // Half-complex keeps one untangle per slot: its mirrored 8-byte stores
+    // would start off the 64-byte boundaries its direct stores keep (measured
+    // slower, 2^7 0.85 -> 0.66 of HBM), so it writes X[k] and X[k + M] only.
+    constexpr bool HALF_ONLY = OUTK == OUT_HALF;
+    constexpr bool NO_HALF = OUTK == OUT_POWER || OUTK == OUT_POWER_SERIAL || OUTK == OUT_PLANES;
+    static_for<0, NO_HALF ? R / 2 + 1 : R>([&](auto uc) {
         constexpr int u = decltype(uc)::value;
         const float2 pu = K::template partner_at<u>(v, buf, t, src);
         if (!active) return;
+        const bool half = HALF_ONLY || (!NO_HALF && outk == OUT_HALF);
+        if (!half) {
+            if (u > R / 2 || (u == R / 2 && t != 0)) return;
+        }
         const int k = t + u * T;
         float2 e, wo;
         K::untangle(v[u], pu, tw_get(tw, k, k), e, wo);
         const float2 xa = cadd(e, wo);  // X[k]
+        const float2 xb = csub(e, wo);  // X[k + M]
+        const bool mid = u == R / 2;     // k = M/2 (power): X[k + M] = X[N - k]
         if (outk == OUT_POWER || outk == OUT_POWER_SERIAL) {
             const bool ser = OUTK == OUT_POWER_SERIAL || (OUTK == OUT_RUNTIME && outk == OUT_POWER_SERIAL);
-            const float p = ser ? power_of<OUT_POWER_SERIAL>(xa) : power_of<OUT_POWER>(xa);
-            const float2 xb = csub(e, wo);
+            const float pa = ser ? power_of<OUT_POWER_SERIAL>(xa) : power_of<OUT_POWER>(xa);
             if (!a.dense) {
                 float* row = a.out + f * (uint64_t)N;
-                __stcs(row + k, p);
-                if (k != 0) __stcs(row + (N - k), p);  // |X[N-k]| = |X[k]| for real frames
-                else __stcs(row + M, ser ? power_of<OUT_POWER_SERIAL>(xb) : power_of<OUT_POWER>(xb));
+                __stcs(row + k, pa);
+                if (k != 0) __stcs(row + (N - k), pa);  // |X[N-k]| = |X[k]|
+                if (!mid) {
+                    const float pb = ser ? power_of<OUT_POWER_SERIAL>(xb) : power_of<OUT_POWER>(xb);
+                    __stcs(row + (M + k), pb);
+                    if (k != 0) __stcs(row + (M - k), pb);  // |X[M-k]| = |X[M+k]|
+                }
             } else {
                 float* row = a.out + f * (uint64_t)(M + 1);
-                __stcs(row + k, p);
-                if (k == 0) __stcs(row + M, ser ? power_of<OUT_POWER_SERIAL>(xb) : power_of<OUT_POWER>(xb));
+                __stcs(row + k, pa);
+                if (!mid) __stcs(row + (M - k), ser ? power_of<OUT_POWER_SERIAL>(xb) : power_of<OUT_POWER>(xb));
             }
         } else if (outk == OUT_HALF) {
-            const float2 xb = csub(e, wo);  // X[k + M]
             float2* o2 = reinterpret_cast<float2*>(a.out);
             if (!a.dense) {
                 const uint64_t flat = f * (uint64_t)N + k;
@@ -436,12 +453,17 @@ __device__ __forceinline__ void fused_group_frames(const FusedArgs& a, uint64_t 
                 if (k == 0) __stcs(row + M, xb);
             }
         } else {  // planes
-            const float2 xb = csub(e, wo);
-            const uint64_t b = f * (uint64_t)N + k;
-            a.out[b] = xa.x;
-            a.out_im[b] = xa.y;
-            a.out[b + M] = xb.x;
-            a.out_im[b + M] = xb.y;
+            const uint64_t b = f * (uint64_t)N;
+            a.out[b + k] = xa.x;
+            a.out_im[b + k] = xa.y;
+            a.out[b + k + M] = xb.x;
+            a.out_im[b + k + M] = xb.y;
+            if (!mid && k != 0) {
+                a.out[b + (N - k)] = xa.x;
+                a.out_im[b + (N - k)] = -xa.y;
+                a.out[b + (M - k)] = xb.x;
+                a.out_im[b + (M - k)] = -xb.y;
+            }
         }
     });
 }
@@ -609,25 +631,34 @@ stft_staged_kernel(const FusedArgs a)
         __syncthreads();  // exchange buffers become output rows
 
         // ---------------- untangle into padded output rows
+        // power: bins k < M/2 give X[k], X[N-k], X[M+k], X[M-k] (k = M/2 by
+        // thread 0); half-complex: X[k] and X[k + M] for every slot
         float* orow = s_x + lf * OS;
-        static_for<0, R>([&](auto uc) {
+        static_for<0, OUTK == OUT_HALF ? R : R / 2 + 1>([&](auto uc) {
             constexpr int u = decltype(uc)::value;
             float2 pu;
             if constexpr (T > 32) pu = pz[u];
             else pu = K::template partner_at<u>(v, buf, t, src);
+            if constexpr (OUTK != OUT_HALF && u == R / 2) {
+                if (t != 0) return;
+            }
             const int k = t + u * T;
             float2 e, wo;
             K::untangle(v[u], pu, tw_get(tw, k, k), e, wo);
-            const float2 xa = cadd(e, wo);
+            const float2 xa = cadd(e, wo), xb = csub(e, wo);
             if constexpr (OUTK == OUT_HALF) {
                 float2* o2 = reinterpret_cast<float2*>(orow);
                 o2[k] = xa;
-                o2[k + M] = csub(e, wo);
+                o2[k + M] = xb;
             } else {
-                const float p = power_of<OUTK>(xa);
-                orow[k] = p;
-                if (k != 0) orow[N - k] = p;
-                else orow[M] = power_of<OUTK>(csub(e, wo));
+                const float pa = power_of<OUTK>(xa);
+                orow[k] = pa;
+                if (k != 0) orow[N - k] = pa;
+                if constexpr (u != R / 2) {
+                    const float pb = power_of<OUTK>(xb);
+                    orow[M + k] = pb;
+                    if (k != 0) orow[M - k] = pb;
+                }
             }
         });
         __syncthreads();
