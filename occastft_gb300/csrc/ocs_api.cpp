@@ -399,32 +399,36 @@ int get_two_level(uint64_t L, const float2** lo, const float2** hi)
     return OCS_OK;
 }
 
-// Windows 2^16 .. 2^22: the two-launch four-step FFT over frames [f0, f1),
-// with a stream-ordered scratch area of at most ~1 GB (frames in chunks).
-int launch_large_frames(const Request& r, const float* d_sig, uint64_t n, float* d_out, uint64_t f0, uint64_t f1,
-                        cudaStream_t st)
+// Windows 2^16 .. 2^30: the four-step FFT (two launches up to 2^22, three
+// above) over frames [f0, f1), with stream-ordered scratch of at most ~1 GB
+// per buffer (frames in chunks; one frame at a time when a frame needs more).
+// win: the scaled window table, or null for no window (the stage hook);
+// out_im: the imaginary plane for the planes output.
+int launch_large_core(int exp, int outk, const float* d_sig, uint64_t n, uint64_t hop, const float* win, int dense,
+                      int remove_dc, uint64_t ohalf, float* d_out, float* d_out_im, uint64_t f0, uint64_t f1,
+                      cudaStream_t st)
 {
     if (f1 <= f0) return OCS_OK;
-    const int e1 = ocs::large_m1_log2(r.exp) + 1, e2 = ocs::large_m2_log2(r.exp) + 1;
+    const ocs::LargePlan pl = ocs::large_plan(exp);
+    if (pl.passes == 0) return fail(OCS_EINVAL, "no four-step plan for this window size");
     ocs::LargeArgs a{};
-    int rc = get_twiddles(e1, false, &a.tw1);
-    if (!rc) rc = get_twiddles(e2, false, &a.tw2);
-    if (!rc) rc = get_window(r.opt.window, r.exp, r.opt.sigma, true, &a.win);
-    const uint64_t N = r.geo.n_window, M = N / 2;
+    int rc = get_twiddles(pl.l1 + 1, false, &a.tw1);
+    if (!rc) rc = get_twiddles(pl.l3 + 1, false, &a.tw2);
+    if (!rc && pl.passes == 3) rc = get_twiddles(pl.l2 + 1, false, &a.tw3);
+    const uint64_t N = 1ull << exp, M = N / 2;
     if (!rc) rc = get_two_level(M, &a.twm_lo, &a.twm_hi);
     if (!rc) rc = get_two_level(N, &a.twn_lo, &a.twn_hi);
     if (rc) return rc;
     a.x = d_sig;
     a.n = n;
-    a.hop = r.geo.hop;
+    a.hop = hop;
     a.frames_total = f1;
+    a.win = win;
     a.out = d_out;
-    a.ohalf = r.opt.half_complex && !r.opt.dense ? (uint64_t)r.geo.ohalf : 0;
-    a.dense = r.opt.dense;
-    a.remove_dc = r.opt.remove_dc;
-    a.m1 = 1ull << (e1 - 1);
-    a.m2 = 1ull << (e2 - 1);
-    const int outk = r.opt.half_complex ? ocs::OUT_HALF : (r.opt.serial_power ? ocs::OUT_POWER_SERIAL : ocs::OUT_POWER);
+    a.out_im = d_out_im;
+    a.ohalf = ohalf;
+    a.dense = dense;
+    a.remove_dc = remove_dc;
     // scratch per chunk (OCS_LARGE_SCRATCH_MB overrides).  Measured on GB300
     // at 1e8 samples: chunks small enough for the scratch to stay in L2
     // (16-96 MB) lose to fewer, fuller launch pairs; 1 GB is the default
@@ -433,17 +437,35 @@ int launch_large_frames(const Request& r, const float* d_sig, uint64_t n, float*
         scratch_bytes = (uint64_t)std::min(std::max(1L, std::atol(sb)), 1L << 20) << 20;  // 1 MB .. 1 TB
     const uint64_t per = std::max<uint64_t>(1, std::min<uint64_t>(f1 - f0, scratch_bytes / (M * sizeof(float2))));
     float2* scratch = nullptr;
+    float2* scratch2 = nullptr;
     OCS_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&scratch), per * M * sizeof(float2), st));
-    a.scratch = scratch;
     cudaError_t e = cudaSuccess;
+    if (pl.passes == 3) e = cudaMallocAsync(reinterpret_cast<void**>(&scratch2), per * M * sizeof(float2), st);
+    a.scratch = scratch;
+    a.scratch2 = scratch2;
     for (uint64_t c0 = f0; c0 < f1 && e == cudaSuccess; c0 += per) {
         a.f0 = c0;
-        e = ocs::launch_large(r.exp, outk, a, std::min(per, f1 - c0), st);
+        e = ocs::launch_large(exp, outk, a, std::min(per, f1 - c0), st);
     }
     const cudaError_t e2b = cudaFreeAsync(scratch, st);
+    const cudaError_t e3b = scratch2 ? cudaFreeAsync(scratch2, st) : cudaSuccess;
     if (e != cudaSuccess) return cuda_fail(e, "large-window launch");
     if (e2b != cudaSuccess) return cuda_fail(e2b, "large-window scratch");
+    if (e3b != cudaSuccess) return cuda_fail(e3b, "large-window scratch");
     return OCS_OK;
+}
+
+int launch_large_frames(const Request& r, const float* d_sig, uint64_t n, float* d_out, uint64_t f0, uint64_t f1,
+                        cudaStream_t st)
+{
+    if (f1 <= f0) return OCS_OK;
+    const float* win = nullptr;
+    int rc = get_window(r.opt.window, r.exp, r.opt.sigma, true, &win);
+    if (rc) return rc;
+    const int outk = r.opt.half_complex ? ocs::OUT_HALF : (r.opt.serial_power ? ocs::OUT_POWER_SERIAL : ocs::OUT_POWER);
+    return launch_large_core(r.exp, outk, d_sig, n, r.geo.hop, win, r.opt.dense, r.opt.remove_dc,
+                             r.opt.half_complex && !r.opt.dense ? (uint64_t)r.geo.ohalf : 0, d_out, nullptr, f0, f1,
+                             st);
 }
 
 // Launch the fused kernel for frames [f0, f1) of a request.  The first launch
@@ -1159,7 +1181,7 @@ int ocs_stage_window(int kind, float* d_data, uint32_t ofull, uint32_t window_si
         return fail(OCS_EINVAL, "window: bad arguments");
     int exp = 0;
     while ((1u << exp) < window_size) ++exp;
-    if (exp > 15) return fail(OCS_EINVAL, "window: size above 2^15");
+    if (exp > ocs::kLargeMaxExp) return fail(OCS_EINVAL, "window: size above 2^30");
     int rc = ensure_init();
     if (rc) return rc;
     const float* w = nullptr;
@@ -1182,10 +1204,20 @@ int ocs_stage_remove_dc(float* d_data, uint32_t qt, uint32_t ofull, uint32_t win
 int ocs_stage_fft(float* d_real, float* d_imag, uint32_t ohalf, uint32_t exp, void* stream)
 {
     if (exp < 6) return fail(OCS_EINVAL, "Operation not supported");
-    if (exp > 15) return fail(OCS_EINVAL, "Operation not supported: window sizes above 2^15");
+    if (exp > (uint32_t)ocs::kLargeMaxExp) return fail(OCS_EINVAL, "Operation not supported: window sizes above 2^30");
     if (!d_real || !d_imag) return fail(OCS_EINVAL, "EXP: null buffer");
     int rc = ensure_init();
     if (rc) return rc;
+    if (ocs::large_supports((int)exp)) {
+        // EXPC above the one-launch sizes: the four-step FFT of every frame of
+        // the real plane, no window, full N-bin spectra into both planes.  The
+        // frames are chunked and each chunk's column pass reads its frames
+        // before its row pass writes them, so the transform runs in place.
+        const uint64_t N = 1ull << exp;
+        const uint64_t frames = 2ull * ohalf / N;
+        return launch_large_core((int)exp, ocs::OUT_PLANES, d_real, 2ull * ohalf, N, nullptr, 0, 0, 0, d_real, d_imag,
+                                 0, frames, (cudaStream_t)stream);
+    }
     const float2* tw = nullptr;
     rc = get_twiddles((int)exp, false, &tw);
     if (rc) return rc;

@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <thread>
 
 namespace ocs {
 
@@ -60,11 +61,13 @@ std::string parse_options(const char* options, Options& o)
 std::string make_geometry(uint64_t n, int exp, float overlap, const Options& o, Geometry& g)
 {
     if (exp < 6) return "Operation not supported";
-    if (exp > 22) return "Operation not supported: window sizes above 2^22";
+    // the reference's window size is an int: 2^31 overflows it, and at 2^30
+    // OFullSize = qt * N < 2^32 already allows at most three frames
+    if (exp > 30) return "Operation not supported: window sizes above 2^30";
     if (n == 0) return "empty input signal";
     if (n > 0xffffffffull) return "signal longer than 2^32-1 samples";
     if (!(overlap < 1.0f) || std::isnan(overlap)) return "overlap ratio must be below 1";
-    const int win = 1 << exp;
+    const uint32_t win = 1u << exp;
     const float hopf = (float)win * (1.0f - overlap);  // CudaImpl.cpp:421
     if (!(hopf >= 1.0f) || hopf >= 4294967296.0f) return "frame advance (OMove) below one sample";
     const float full = (float)(uint32_t)n;
@@ -100,7 +103,10 @@ std::vector<float> window_table(int kind, int nwin, float sigma)
     std::vector<float> w;
     if (kind == WIN_NONE) return w;
     w.resize(nwin);
-    for (int i = 0; i < nwin; ++i) {
+    // every entry is the same float/double expression, so tables of windows
+    // of millions of samples fill in parallel without changing a bit
+    auto fill = [&](int i0, int i1) {
+    for (int i = i0; i < i1; ++i) {
         float v = 1.0f;
         switch (kind) {
         case WIN_HANNING: {
@@ -160,6 +166,20 @@ std::vector<float> window_table(int kind, int nwin, float sigma)
             break;
         }
         w[i] = v;
+    }
+    };
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int parts = (nwin >= (1 << 20) && hw > 1) ? (int)(hw < 64 ? hw : 64) : 1;
+    if (parts == 1) {
+        fill(0, nwin);
+    } else {
+        std::vector<std::thread> th;
+        const int per = (nwin + parts - 1) / parts;
+        for (int p = 0; p < parts; ++p) {
+            const int i0 = p * per, i1 = i0 + per < nwin ? i0 + per : nwin;
+            if (i0 < i1) th.emplace_back(fill, i0, i1);
+        }
+        for (auto& t : th) t.join();
     }
     return w;
 }

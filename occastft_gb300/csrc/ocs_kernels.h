@@ -99,33 +99,46 @@ int tpf_occupancy(int exp, int outk);
 // the kernel as a parameter
 cudaError_t launch_tpf(int exp, int outk, const FusedArgs& a, const float* host_win, int grid, cudaStream_t st);
 
-// windows 2^16 .. 2^22: four-step FFT in two launches (column pass, row pass)
+// windows 2^16 .. 2^30: a four-step FFT of the frame's M = N/2 complex
+// points.  Up to 2^22 it takes two launches (a column pass from the signal,
+// M = M1 * M2, and a row pass that untangles and stores); above, three
+// (M = P1 * P2 * Q: the column pass, a middle pass over P2, the row pass).
+// Output kinds: power, serial power, half-complex, and planes (the stage hook).
 constexpr int kLargeMinExp = 16;
-constexpr int kLargeMaxExp = 22;
+constexpr int kLargeMaxExp = 30;  // OFullSize = qt * N < 2^32 leaves qt <= 3 at 2^30
+struct LargePlan {
+    int passes;  // 2 or 3
+    int l1;      // log2 of the column FFT
+    int l2;      // log2 of the middle FFT (three passes), else 0
+    int l3;      // log2 of the row FFT; l1 + l2 + l3 = exp - 1
+};
 struct LargeArgs {
-    const float* x;          // whole signal
+    const float* x;          // whole signal (or a real plane with hop = N)
     uint64_t n;              // its samples
     uint64_t hop;
     uint64_t f0;             // first frame of this launch (absolute)
     uint64_t frames_total;   // frames below this index are computed
     uint64_t frames_launch;  // frames of this launch (set by launch_large)
-    const float* win;        // window table scaled by 1/2 (N floats)
+    const float* win;        // window table scaled by 1/2 (N floats); null: 1/2 throughout
     float2* scratch;         // frames of this launch x M complex
-    float* out;              // whole output
+    float2* scratch2;        // the same again (three passes only)
+    float* out;              // whole output (or real plane)
+    float* out_im;           // imaginary plane (planes output)
     uint64_t ohalf;          // compat half-complex: complex outputs in total
     int dense;
     int remove_dc;
-    uint64_t m1, m2;         // M = m1 * m2 complex points per frame
-    const float2* tw1;       // Stockham table of the m1-point FFT (plan of window 2 m1)
-    const float2* tw2;       // Stockham table of the m2-point FFT (plan of window 2 m2)
+    uint64_t m1, m2;         // per launch: the pass's FFT length and its column (or row) count
+    uint64_t col_mask;       // column pass: twiddle exponent uses column & col_mask
+    const float2* tw1;       // Stockham table of the column FFT (plan of window 2^(l1+1))
+    const float2* tw2;       // Stockham table of the row FFT (plan of window 2^(l3+1))
+    const float2* tw3;       // Stockham table of the middle FFT (plan of window 2^(l2+1))
     const float2* twm_lo;    // exp(-2 pi i j / M): lo[j % 1024] * hi[j / 1024]
     const float2* twm_hi;
     const float2* twn_lo;    // exp(-2 pi i k / N), same split
     const float2* twn_hi;
 };
 bool large_supports(int exp);
-int large_m1_log2(int exp);
-int large_m2_log2(int exp);
+LargePlan large_plan(int exp);
 cudaError_t build_two_level(float2* lo, float2* hi, uint64_t L, cudaStream_t st);
 cudaError_t launch_large(int exp, int outk, const LargeArgs& a, uint64_t frames, cudaStream_t st);
 

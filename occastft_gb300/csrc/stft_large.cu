@@ -1,4 +1,5 @@
-// STFT for windows 2^16 .. 2^22 (sm_103a): a four-step FFT in two launches.
+// STFT for windows 2^16 .. 2^30 (sm_103a): a four-step FFT in two launches
+// up to 2^22, three above.
 //
 // One frame of N real samples is the M = N/2 point complex FFT of
 // z[m] = y[2m] + i y[2m+1] plus the real-input untangle, as in the fused
@@ -18,6 +19,16 @@
 // stands in for the mirror of row 0), so every Z[M-k] it needs is its own.
 // It runs 16 M2-point FFTs, then writes outputs with lanes over k1, i.e. 8
 // consecutive bins per (k2) run.
+//
+// Above 2^22 the column FFT would exceed a CTA, so M = P1 * P2 * Q and the
+// column length P = P1 * P2 splits once more (m = c + Q (a + P2 m1),
+// k1 = k1a + P1 k1b):
+//   column pass  U[k1a][c + Q a] = W_P^{a k1a} sum_{m1} z[c + Q a + Q P2 m1] W_{P1}^{m1 k1a}
+//   middle pass  Y[k1a + P1 k1b][c] = W_M^{c k1} sum_a U[k1a][c + Q a] W_{P2}^{a k1b}
+//   row pass     as above, over P rows of Q points.
+// The column pass is the two-launch column pass with Q P2 columns and the
+// twiddle exponent taken from the column's block (c + Q a) & ~(Q - 1) = Q a,
+// since W_P^{a k1a} = W_M^{Q a k1a}.
 //
 // DC removal subtracts the mean of the windowed frame; in the transform that
 // changes bin 0 only (to zero), which is what the row pass writes.  The
@@ -69,6 +80,12 @@ __host__ __device__ constexpr bool large_col_cache_win(int exp1)
 }
 __host__ __device__ constexpr int large_col_frames(int exp1) { return large_col_cache_win(exp1) ? 4 : 1; }
 
+// four window coefficients at real index i (a multiple of 4); no table: 1/2
+__device__ __forceinline__ float4 large_win4(const float* win, uint32_t i)
+{
+    return win ? *reinterpret_cast<const float4*>(win + i) : make_float4(0.5f, 0.5f, 0.5f, 0.5f);
+}
+
 template <int EXP1>
 __global__ void __launch_bounds__(kTileC * (fused_M(EXP1) / fused_cfg(EXP1).R))
     large_columns_kernel(const LargeArgs a)
@@ -96,8 +113,7 @@ __global__ void __launch_bounds__(kTileC * (fused_M(EXP1) / fused_cfg(EXP1).R))
 #pragma unroll
         for (int j = 0; j < NE; ++j) {
             const int e = tid + j * NT, m1 = e >> 2, q = e & 3;
-            wv[j] = *reinterpret_cast<const float4*>(a.win + 2u * ((uint32_t)c0 + (uint32_t)M2 * (uint32_t)m1) +
-                                                     4u * (uint32_t)q);
+            wv[j] = large_win4(a.win, 2u * ((uint32_t)c0 + (uint32_t)M2 * (uint32_t)m1) + 4u * (uint32_t)q);
         }
     }
     const int col = tid / T, t = tid % T;
@@ -129,7 +145,7 @@ __global__ void __launch_bounds__(kTileC * (fused_M(EXP1) / fused_cfg(EXP1).R))
             } else {
                 for (int e = tid; e < M1 * 4; e += NT) {
                     const uint32_t i = 2u * ((uint32_t)c0 + (uint32_t)M2 * (uint32_t)(e >> 2)) + 4u * (uint32_t)(e & 3);
-                    chunk(e, *reinterpret_cast<const float4*>(a.win + i));
+                    chunk(e, large_win4(a.win, i));
                 }
             }
         } else {
@@ -144,7 +160,7 @@ __global__ void __launch_bounds__(kTileC * (fused_M(EXP1) / fused_cfg(EXP1).R))
                     if (g < a.n) xr = a.x[g];
                     if (g + 1 < a.n) xi = a.x[g + 1];
                 }
-                const float2 w = *reinterpret_cast<const float2*>(a.win + i);
+                const float2 w = a.win ? *reinterpret_cast<const float2*>(a.win + i) : make_float2(0.5f, 0.5f);
                 sbuf[cc * BS + K::pd(m1)] = make_float2(xr * w.x, xi * w.y);
             }
         }
@@ -156,12 +172,13 @@ __global__ void __launch_bounds__(kTileC * (fused_M(EXP1) / fused_cfg(EXP1).R))
         __syncthreads();
         // W_M^{c k1}, k1 = t + u T: a two-level lookup at u = 0 and 8, then
         // products with W_M^{c T} (at most 7 rounding steps)
-        const float2 step = tw2l(a.twm_lo, a.twm_hi, c * (uint64_t)T);
+        const uint64_t ce = c & a.col_mask;  // c, or the block Q a of the three-pass form
+        const float2 step = tw2l(a.twm_lo, a.twm_hi, ce * (uint64_t)T);
         float2 w = make_float2(1.0f, 0.0f);
 #pragma unroll
         for (int u = 0; u < R; ++u) {
             const int k1 = t + u * T;
-            w = (u % 8 == 0) ? tw2l(a.twm_lo, a.twm_hi, c * (uint64_t)k1) : cmul(w, step);
+            w = (u % 8 == 0) ? tw2l(a.twm_lo, a.twm_hi, ce * (uint64_t)k1) : cmul(w, step);
             buf[K::pd(k1)] = cmul(v[u], w);
         }
         __syncthreads();
@@ -173,6 +190,63 @@ __global__ void __launch_bounds__(kTileC * (fused_M(EXP1) / fused_cfg(EXP1).R))
             const float2 lo = sbuf[(2 * q) * BS + K::pd(k1)], hi = sbuf[(2 * q + 1) * BS + K::pd(k1)];
             *reinterpret_cast<float4*>(y + (uint64_t)k1 * M2 + c0 + 2 * q) = make_float4(lo.x, lo.y, hi.x, hi.y);
         }
+    }
+}
+
+// ---------------------------------------------------------------- middle pass
+// Three-pass form: a CTA owns 8 consecutive columns c of block k1a of one
+// frame.  It reads rows a (P2 of them, 8 complex values = 64 bytes each, at
+// U + k1a Q P2 + Q a + c0), runs 8 P2-point FFTs on the Stockham core,
+// multiplies W_M^{c (k1a + P1 k1b)} and writes rows k1a + P1 k1b of Y.
+// Per launch: m1 = P1, m2 = Q, scratch = U, scratch2 = Y.
+template <int EXPM>
+__global__ void __launch_bounds__(kTileC * (fused_M(EXPM) / fused_cfg(EXPM).R))
+    large_middle_kernel(const LargeArgs a)
+{
+    using K = Core<EXPM>;
+    constexpr int P2 = K::M, R = K::R, T = K::T;
+    constexpr int NT = kTileC * T;
+    constexpr int BS = large_col_stride(EXPM);
+    extern __shared__ float2 sbuf[];
+    const int tid = threadIdx.x;
+    const uint64_t P1 = a.m1, Q = a.m2;
+    const uint64_t M = P1 * (uint64_t)P2 * Q;
+    const uint64_t ctiles = Q / kTileC;
+    const uint64_t c0 = (blockIdx.x % ctiles) * kTileC;
+    const uint64_t k1a = (blockIdx.x / ctiles) % P1;
+    const uint64_t fl = blockIdx.x / (ctiles * P1);
+    const float2* u = a.scratch + fl * M + k1a * (Q * P2);
+    for (int e = tid; e < P2 * 4; e += NT) {
+        const int r = e >> 2, q = e & 3;
+        const float4 d = *reinterpret_cast<const float4*>(u + (uint64_t)r * Q + c0 + 2 * q);
+        sbuf[(2 * q) * BS + K::pd(r)] = make_float2(d.x, d.y);
+        sbuf[(2 * q + 1) * BS + K::pd(r)] = make_float2(d.z, d.w);
+    }
+    __syncthreads();
+    const int col = tid / T, t = tid % T;
+    float2* buf = sbuf + col * BS;
+    const uint64_t c = c0 + col;
+    float2 v[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i) v[i] = buf[K::pd(t + i * T)];
+    K::fft(v, buf, a.tw3, t);  // slot i: output k1b = t + i T
+    __syncthreads();
+    // W_M^{c (k1a + P1 k1b)}: a two-level lookup at i = 0 and 8, products with
+    // W_M^{c P1 T} between (exponents below M: c < Q, k1a + P1 k1b < P1 P2)
+    const float2 step = tw2l(a.twm_lo, a.twm_hi, c * P1 * (uint64_t)T);
+    float2 w = make_float2(1.0f, 0.0f);
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        const int k1b = t + i * T;
+        w = (i % 8 == 0) ? tw2l(a.twm_lo, a.twm_hi, c * (k1a + P1 * (uint64_t)k1b)) : cmul(w, step);
+        buf[K::pd(k1b)] = cmul(v[i], w);
+    }
+    __syncthreads();
+    float2* y = a.scratch2 + fl * M;
+    for (int e = tid; e < P2 * 4; e += NT) {
+        const int kb = e >> 2, q = e & 3;
+        const float2 lo = sbuf[(2 * q) * BS + K::pd(kb)], hi = sbuf[(2 * q + 1) * BS + K::pd(kb)];
+        *reinterpret_cast<float4*>(y + (k1a + P1 * (uint64_t)kb) * Q + c0 + 2 * q) = make_float4(lo.x, lo.y, hi.x, hi.y);
     }
 }
 
@@ -249,7 +323,12 @@ __global__ void __launch_bounds__(2 * kTileR * (fused_M(EXP2) / fused_cfg(EXP2).
             float2 X0 = make_float2(ev.x + wo.x, ev.y + wo.y);        // X[k]
             const float2 X1 = make_float2(ev.x - wo.x, ev.y - wo.y);  // X[k + M]
             if (dc && k == 0) X0 = make_float2(0.0f, 0.0f);
-            if constexpr (OUTK == OUT_HALF) {
+            if constexpr (OUTK == OUT_PLANES) {
+                a.out[f * N + k] = X0.x;
+                a.out_im[f * N + k] = X0.y;
+                a.out[f * N + k + M] = X1.x;
+                a.out_im[f * N + k + M] = X1.y;
+            } else if constexpr (OUTK == OUT_HALF) {
                 if (!a.dense) {
                     const uint64_t flat = f * N + k;
                     if (flat < a.ohalf) __stcs(o2 + flat, X0);
@@ -322,6 +401,55 @@ cudaError_t launch_rows_e(int outk, const LargeArgs& a, uint64_t frames, cudaStr
     case OUT_POWER: return launch_rows_t<EXP2, OUT_POWER>(a, frames, st);
     case OUT_POWER_SERIAL: return launch_rows_t<EXP2, OUT_POWER_SERIAL>(a, frames, st);
     case OUT_HALF: return launch_rows_t<EXP2, OUT_HALF>(a, frames, st);
+    case OUT_PLANES: return launch_rows_t<EXP2, OUT_PLANES>(a, frames, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+template <int EXPM>
+cudaError_t launch_middle_t(const LargeArgs& a, uint64_t frames, cudaStream_t st)
+{
+    constexpr int T = fused_M(EXPM) / fused_cfg(EXPM).R;
+    constexpr size_t smem = (size_t)kTileC * large_col_stride(EXPM) * sizeof(float2);
+    const cudaError_t e = ensure_smem_attr<large_middle_kernel<EXPM>>(smem);
+    if (e != cudaSuccess) return e;
+    const uint64_t grid = frames * a.m1 * (a.m2 / kTileC);
+    large_middle_kernel<EXPM><<<(unsigned)grid, kTileC * T, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_columns(int l1, const LargeArgs& a, uint64_t frames, cudaStream_t st)
+{
+    switch (l1 + 1) {  // EXP1: the column FFT is the core of window 2^EXP1
+    case 9: return launch_columns_t<9>(a, frames, st);
+    case 10: return launch_columns_t<10>(a, frames, st);
+    case 11: return launch_columns_t<11>(a, frames, st);
+    case 12: return launch_columns_t<12>(a, frames, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_rows(int l3, int outk, const LargeArgs& a, uint64_t frames, cudaStream_t st)
+{
+    switch (l3 + 1) {
+    case 8: return launch_rows_e<8>(outk, a, frames, st);
+    case 9: return launch_rows_e<9>(outk, a, frames, st);
+    case 10: return launch_rows_e<10>(outk, a, frames, st);
+    case 11: return launch_rows_e<11>(outk, a, frames, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_middle(int l2, const LargeArgs& a, uint64_t frames, cudaStream_t st)
+{
+    switch (l2 + 1) {
+    case 6: return launch_middle_t<6>(a, frames, st);
+    case 7: return launch_middle_t<7>(a, frames, st);
+    case 8: return launch_middle_t<8>(a, frames, st);
+    case 9: return launch_middle_t<9>(a, frames, st);
+    case 10: return launch_middle_t<10>(a, frames, st);
+    case 11: return launch_middle_t<11>(a, frames, st);
+    case 12: return launch_middle_t<12>(a, frames, st);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -329,8 +457,23 @@ cudaError_t launch_rows_e(int outk, const LargeArgs& a, uint64_t frames, cudaStr
 }  // namespace
 
 bool large_supports(int exp) { return exp >= kLargeMinExp && exp <= kLargeMaxExp; }
-int large_m1_log2(int exp) { return large_l1(exp); }
-int large_m2_log2(int exp) { return large_l2(exp); }
+
+// Two passes up to 2^22 (column FFT 2^(exp/2), rows of the rest).  Above,
+// rows of Q = 2^l3 points (l3 <= 10, the largest row pass), a column FFT of
+// 2^l1 (8 <= l1 <= 11) and a middle FFT of 2^l2 (5 <= l2 <= 11), l1 >= l2 as
+// close as the ranges allow.
+LargePlan large_plan(int exp)
+{
+    if (exp <= 22) return LargePlan{2, large_l1(exp), 0, large_l2(exp)};
+    const int total = exp - 1;
+    for (int l3 = 10; l3 >= 7; --l3) {
+        const int rest = total - l3;
+        const int l1 = (rest + 1) / 2 < 8 ? 8 : ((rest + 1) / 2 > 11 ? 11 : (rest + 1) / 2);
+        const int l2 = rest - l1;
+        if (l2 >= 5 && l2 <= 11) return LargePlan{3, l1, l2, l3};
+    }
+    return LargePlan{0, 0, 0, 0};
+}
 
 cudaError_t build_two_level(float2* lo, float2* hi, uint64_t L, cudaStream_t st)
 {
@@ -342,22 +485,27 @@ cudaError_t build_two_level(float2* lo, float2* hi, uint64_t L, cudaStream_t st)
 cudaError_t launch_large(int exp, int outk, const LargeArgs& a, uint64_t frames, cudaStream_t st)
 {
     if (!large_supports(exp) || frames == 0) return cudaErrorInvalidValue;
-    cudaError_t e;
-    switch (large_l1(exp) + 1) {  // EXP1: the M1-point FFT is the core of window 2^EXP1
-    case 9: e = launch_columns_t<9>(a, frames, st); break;
-    case 10: e = launch_columns_t<10>(a, frames, st); break;
-    case 11: e = launch_columns_t<11>(a, frames, st); break;
-    case 12: e = launch_columns_t<12>(a, frames, st); break;
-    default: return cudaErrorInvalidValue;
-    }
+    const LargePlan pl = large_plan(exp);
+    if (pl.passes == 0) return cudaErrorInvalidValue;
+    const uint64_t q = 1ull << pl.l3;
+    LargeArgs c = a;  // column pass: FFT of 2^l1, columns = M / 2^l1
+    c.m1 = 1ull << pl.l1;
+    c.m2 = 1ull << (pl.l2 + pl.l3);
+    c.col_mask = pl.passes == 3 ? ~(q - 1) : ~0ull;
+    cudaError_t e = launch_columns(pl.l1, c, frames, st);
     if (e != cudaSuccess) return e;
-    switch (large_l2(exp) + 1) {
-    case 8: return launch_rows_e<8>(outk, a, frames, st);
-    case 9: return launch_rows_e<9>(outk, a, frames, st);
-    case 10: return launch_rows_e<10>(outk, a, frames, st);
-    case 11: return launch_rows_e<11>(outk, a, frames, st);
-    default: return cudaErrorInvalidValue;
+    LargeArgs r = a;  // row pass: rows of Q points, M / Q of them
+    r.m1 = 1ull << (pl.l1 + pl.l2);
+    r.m2 = q;
+    if (pl.passes == 3) {
+        LargeArgs m = a;
+        m.m1 = 1ull << pl.l1;
+        m.m2 = q;
+        e = launch_middle(pl.l2, m, frames, st);
+        if (e != cudaSuccess) return e;
+        r.scratch = a.scratch2;
     }
+    return launch_rows(pl.l3, outk, r, frames, st);
 }
 
 }  // namespace ocs

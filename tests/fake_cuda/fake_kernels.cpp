@@ -101,8 +101,11 @@ cudaError_t launch_tpf(int exp, int outk, const FusedArgs& a, const float* host_
 }
 
 bool large_supports(int exp) { return exp >= kLargeMinExp && exp <= kLargeMaxExp; }
-int large_m1_log2(int exp) { return (exp - 1) / 2; }
-int large_m2_log2(int exp) { return (exp - 1) - (exp - 1) / 2; }
+LargePlan large_plan(int exp)
+{
+    if (exp <= 22) return LargePlan{2, exp / 2, 0, exp - 1 - exp / 2};
+    return LargePlan{3, 8, exp - 1 - 8 - 10, 10};
+}
 cudaError_t build_two_level(float2*, float2*, uint64_t, cudaStream_t) { return no_work(); }
 cudaError_t launch_large(int exp, int outk, const LargeArgs& a, uint64_t frames, cudaStream_t st)
 {

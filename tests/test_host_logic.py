@@ -113,12 +113,19 @@ def test_gaussian_sigma_quirk(ocs_lib, orc):
 
 
 def test_window_exponent_limits(ocs_lib):
-    """Windows up to 2^22 are accepted (the reference's EXPC has no upper
-    bound short of OFullSize < 2^32); 2^23 is refused with a status."""
+    """Every window the reference's EXPC takes is accepted: exponents up to
+    30, as long as OFullSize = qt * N stays below 2^32 (RunnerCommon.cpp:290-306);
+    2^31 overflows the reference's int window size and is refused."""
     g = ocs_lib.geometry(50_000_000, 22, 0.5, "--hanning_window")
     assert g.n_window == 1 << 22 and g.out_floats == g.qt * (1 << 22)
-    with pytest.raises(ocs_lib.OcsError, match="above 2\\^22"):
-        ocs_lib.geometry(50_000_000, 23, 0.5, "")
+    g = ocs_lib.geometry(50_000_000, 23, 0.5, "")
+    assert g.n_window == 1 << 23 and g.qt == 50_000_000 // (1 << 22) + 1
+    g = ocs_lib.geometry(1 << 31, 30, 0.0, "--blackman_window")
+    assert g.qt == 3 and g.ofull == 3 << 30
+    with pytest.raises(ocs_lib.OcsError, match="OFullSize"):
+        ocs_lib.geometry(1 << 31, 30, 0.5, "")
+    with pytest.raises(ocs_lib.OcsError, match="above 2\\^30"):
+        ocs_lib.geometry(50_000_000, 31, 0.5, "")
 
 
 def test_python_pointer_arguments_are_checked(ocs_lib):
@@ -186,11 +193,11 @@ def test_validation_before_any_device_call(ocs_lib):
 
     # per-stage hooks (runnerFunction::*)
     err(L.ocs_stage_fft(P, P, 1024, 5, None), ocs_lib.OCS_EINVAL, "Operation not supported")
-    err(L.ocs_stage_fft(P, P, 1024, 16, None), ocs_lib.OCS_EINVAL, "above 2^15")
+    err(L.ocs_stage_fft(P, P, 1024, 31, None), ocs_lib.OCS_EINVAL, "above 2^30")
     err(L.ocs_stage_fft(None, P, 1024, 10, None), ocs_lib.OCS_EINVAL, "null buffer")
     err(L.ocs_stage_window(0, P, 1024, 1024, -1.0, None), ocs_lib.OCS_EINVAL, "window")
     err(L.ocs_stage_window(1, P, 1024, 1000, -1.0, None), ocs_lib.OCS_EINVAL, "window")
-    err(L.ocs_stage_window(1, P, 1 << 17, 1 << 16, -1.0, None), ocs_lib.OCS_EINVAL, "above 2^15")
+    err(L.ocs_stage_window(1, P, 1 << 31, 1 << 31, -1.0, None), ocs_lib.OCS_EINVAL, "above 2^30")
     err(L.ocs_stage_remove_dc(None, 1, 1024, 1024, None), ocs_lib.OCS_EINVAL, "RemoveDC")
     err(L.ocs_stage_overlap(P, 1024, 1000, 5, 512, P, None), ocs_lib.OCS_EINVAL, "Overlap")
     err(L.ocs_stage_half_complex(None, P, P, 512, 10, None), ocs_lib.OCS_EINVAL, "HalfComplex")

@@ -53,3 +53,23 @@ def test_port_at_reference_cost_matches_reference(orc):
             assert np.array_equal(ref.view(np.uint32), mine.view(np.uint32)), (exp, op)
     finally:
         orc.set_reference_cost(False)
+
+
+@ref_missing
+def test_reference_serial_twiddle_overflow_from_2pow17(orc):
+    """The reference's own Serial runner is not the DFT from window 2^17 on:
+    its twiddle index (lsave % segmentSize) * HwindowSize (OKL/kernel.okl:141-144)
+    overflows a 32-bit int once segmentSize * N/2 reaches 2^31.  The oracle's
+    restatement reproduces the same bits; the FP64 oracle is the accuracy
+    reference at those sizes."""
+    R = orc.RefLib("libref_serial.so")
+    for exp, bad in ((16, False), (18, True)):
+        N = 1 << exp
+        x = signal(5, 3 * N + 7)
+        opts = "--hamming_window --half_complex_return"
+        ref, st = R.activate(x, exp, 0.5, opts)
+        assert st == "OK"
+        mine = orc.serial_pipeline(x, exp, 0.5, opts, nthreads=4)
+        assert np.array_equal(ref.view(np.uint32), mine.view(np.uint32))
+        err = orc.rel_l2(ref, orc.fp64_stft(x, exp, 0.5, opts))
+        assert (err > 0.1) if bad else (err < 1e-6), (exp, err)
