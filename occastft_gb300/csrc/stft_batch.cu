@@ -133,15 +133,17 @@ __device__ __forceinline__ void batch_tile(const FusedArgs& a, uint64_t f0, uint
     FusedArgs b = a;
     b.frames = f0 + nf;  // frames past the tile belong to the next tile
     // The output kind is the same for the whole tile.  Power tiles get a body
-    // specialised for it, except at 2^11 and 2^13, where the extra body makes
-    // the kernel spill under its 128-register cap (2^11 tiles fell from 0.49
-    // to 0.31 of HBM); other kinds take the run-time body.
+    // specialised for it, except at 2^13, where the extra body makes the
+    // kernel spill under its 128-register cap; other kinds take the run-time
+    // body.  (2^11 spilled too until the power body went to four bins per
+    // untangle; now its power tiles run at 0.63 of HBM against 0.50 with the
+    // run-time body.)
     // each frame group prefetches its next frame of the tile into L2
     auto run = [&](const auto& twx) {
-        if (EXP != 11 && EXP != 13 && a.outk == OUT_POWER) {
+        if (EXP != 13 && a.outk == OUT_POWER) {
             for (uint64_t fb = f0; fb < f0 + nf; fb += FPC) {
                 fused_prefetch_next<EXP>(b, fb + FPC + lf, t);
-                fused_group_frames<EXP, (EXP != 11 && EXP != 13) ? OUT_POWER : OUT_RUNTIME>(b, fb, buf, red, twx,
+                fused_group_frames<EXP, (EXP != 13) ? OUT_POWER : OUT_RUNTIME>(b, fb, buf, red, twx,
                                                                                              win2, tid, lf, t);
             }
         } else {
