@@ -18,8 +18,8 @@ __host__ __device__ constexpr size_t batch_group_smem(int exp)
 {
     return (size_t)fused_fpc(exp) * fused_buf_stride(exp) * 8 + (size_t)(256 / 32) * 4 + 16;
 }
-// power tiles of windows 2^9 and 2^10 run the two-frames-per-FFT body
-__host__ __device__ constexpr bool batch_pair_exp(int exp) { return exp == 9 || exp == 10; }
+// power tiles of windows 2^9, 2^10 and 2^12 run the two-frames-per-FFT body
+__host__ __device__ constexpr bool batch_pair_exp(int exp) { return exp == 9 || exp == 10 || exp == 12; }
 __host__ __device__ constexpr size_t batch_pair_smem(int exp)
 {
     return (size_t)pair_ppc(exp) * pair_buf_stride(exp) * 8 + (size_t)(256 / 32) * 8 + 16;
@@ -44,8 +44,9 @@ constexpr int kBatchSmemTabMaxExp = 11;
 __host__ __device__ constexpr size_t batch_tab_smem()
 {
     size_t m = 0;
-    for (int e = kBatchMinExp; e <= kBatchSmemTabMaxExp; ++e) {
-        const size_t b = (size_t)fused_tw_size(e) * 8 + ((size_t)1 << e) * 4;
+    for (int e = kBatchMinExp; e <= kBatchMaxExp; ++e) {
+        const size_t b = e <= kBatchSmemTabMaxExp ? (size_t)fused_tw_size(e) * 8 + ((size_t)1 << e) * 4
+                                                  : fused_tw2_entries(e) * 8;
         m = b > m ? b : m;
         if (batch_pair_exp(e)) m = pair_tab_bytes(e) > m ? pair_tab_bytes(e) : m;
     }
@@ -61,19 +62,31 @@ __device__ __forceinline__ void batch_tile(const FusedArgs& a, uint64_t f0, uint
     if constexpr (batch_pair_exp(EXP)) {
         if (a.outk == OUT_POWER && a.tw_pair) {
             // two frames per FFT: pairs f0/2 .. of the tile (f0 and nf are even
-            // multiples of the CTA's pairs), the pair plan's tables and the
-            // window resident behind the frame buffers
+            // multiples of the CTA's pairs), the pair plan's tables (at 2^12 the
+            // first exchange stage's twiddles and a two-level table for the
+            // later ones) and the window resident behind the frame buffers
             static_assert(pair_cta_threads(EXP) == 256, "batch CTAs have 256 threads");
             constexpr int PPC = pair_ppc(EXP), BS = pair_buf_stride(EXP), T = pair_T(EXP);
             constexpr int TWN = pair_smem_tw_entries(EXP);
             const int tid = threadIdx.x;
             float2* st = reinterpret_cast<float2*>(reinterpret_cast<char*>(smem) + batch_frames_smem());
-            float* sw = reinterpret_cast<float*>(st + TWN);
+            float2* s2 = st + TWN;  // the later stages' two-level table (from 2^12)
+            float* sw = reinterpret_cast<float*>(reinterpret_cast<char*>(s2) + pair_tw2l_bytes(EXP));
             const bool new_tw = *s_tw != a.tw_pair, new_win = *s_win != a.win;
             if (new_tw || new_win) {
                 __syncthreads();  // the previous tile's table reads are over
-                if (new_tw)
+                if (new_tw) {
                     for (int i = tid; i < TWN; i += 256) st[i] = a.tw_pair[i];
+                    if constexpr (pair_tw2l(EXP)) {
+                        // lo[e] = W_N^e (e < 128), hi[h] = W_N^(128 h), as the paired kernel builds them
+                        for (int i = tid; i < 128 + (1 << EXP) / 128; i += 256) {
+                            const int e = i < 128 ? i : (i - 128) * 128;
+                            double sn, cs;
+                            sincospi(2.0 * (double)e / (double)(1 << EXP), &sn, &cs);
+                            s2[i] = make_float2((float)cs, (float)(-sn));
+                        }
+                    }
+                }
                 for (int i = tid; i < (1 << EXP); i += 256) sw[i] = a.win[i];
                 __syncthreads();
                 if (tid == 0) {
@@ -85,7 +98,8 @@ __device__ __forceinline__ void batch_tile(const FusedArgs& a, uint64_t f0, uint
             b.frames = f0 + nf;  // frames past the tile belong to the next tile
             b.tw = a.tw_pair;
             const int lp = tid / T, t = tid - lp * T;
-            const TwTwoLevel tw2{nullptr, nullptr};
+            TwTwoLevel tw2{nullptr, nullptr};
+            if constexpr (pair_tw2l(EXP)) tw2 = TwTwoLevel{s2, s2 + 128};
             for (uint64_t pbase = f0 / 2; 2 * pbase < f0 + nf; pbase += PPC) {
                 const uint64_t q = pbase + PPC + lp;  // this group's next pair in the tile
                 if (t == 0 && 2 * q < b.frames) {
