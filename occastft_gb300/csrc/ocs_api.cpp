@@ -781,6 +781,8 @@ int batch_build(ocs_request* reqs, int count, BatchPlan& bp, bool write_status)
         a.dense = r.opt.dense;
         a.remove_dc = r.opt.remove_dc;
         a.vec2 = (r.geo.hop % 2 == 0) && ((reinterpret_cast<uintptr_t>(q.in) & 7u) == 0);
+        // bytes per async copy of the lanes-per-frame tiles (2^7, 2^8 power)
+        a.cs = ((r.geo.hop % 4 == 0) && (reinterpret_cast<uintptr_t>(q.in) & 15u) == 0) ? 16 : (a.vec2 ? 8 : 4);
         a.exp = r.exp;
         a.outk = outk_of(i);
         const uint32_t idx = (uint32_t)bp.descs.size();

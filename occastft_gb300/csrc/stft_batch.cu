@@ -8,6 +8,7 @@
 // kind) on the host so that concurrently running CTAs mostly share one code
 // path.
 #include "stft_pair_kernel.cuh"
+#include "stft_tpfl_body.cuh"
 
 namespace ocs {
 
@@ -59,6 +60,45 @@ __device__ __forceinline__ void batch_tile(const FusedArgs& a, uint64_t f0, uint
                                            const float2** s_tw, const float** s_win)
 {
     static_assert(fused_cta_threads(EXP) == 256, "batch CTAs have 256 threads");
+    if constexpr (EXP == 7 || EXP == 8) {
+        // power tiles of 2^7 and 2^8: the lanes-per-frame body (N/64 lanes per
+        // frame, the FFT in registers), each warp taking groups of F frames
+        // through its own padded rows in the frame region; its twiddle tables
+        // and the window (as float4s) behind them.  The reference layout needs
+        // a 16-byte-aligned output for its row stores.
+        const bool power = a.outk == OUT_POWER || a.outk == OUT_POWER_SERIAL;
+        if (power && a.cs != 0 && (a.dense || (reinterpret_cast<uintptr_t>(a.out) & 15u) == 0)) {
+            using C = TplCfg<EXP>;
+            constexpr int L = C::L, F = C::F, RS = C::RS, N = C::N;
+            static_assert((size_t)8 * F * RS * 4 <= batch_frames_smem(), "rows fit the frame region");
+            const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+            float2* s_tw1 = reinterpret_cast<float2*>(reinterpret_cast<char*>(smem) + batch_frames_smem());
+            float2* s_tw2 = s_tw1 + 32 * L;
+            float4* sw4 = reinterpret_cast<float4*>(s_tw2 + 17 * L);
+            const float2* marker = reinterpret_cast<const float2*>(&tpl_tab<EXP>());
+            const bool new_tw = *s_tw != marker, new_win = *s_win != a.win;
+            if (new_tw || new_win) {
+                __syncthreads();  // the previous tile's table reads are over
+                if (new_tw) tpl_tables<EXP>(s_tw1, s_tw2, tid, 256);
+                for (int i = tid; i < N / 4; i += 256) sw4[i] = reinterpret_cast<const float4*>(a.win)[i];
+                __syncthreads();
+                if (tid == 0) {
+                    *s_tw = marker;
+                    *s_win = a.win;
+                }
+            }
+            FusedArgs b = a;
+            b.frames = f0 + nf;  // frames past the tile belong to the next tile
+            float* rows = reinterpret_cast<float*>(smem) + warp * F * RS;
+            const float4* w4 = sw4;
+            for (uint64_t g = f0 / F + warp; g * F < f0 + nf; g += 8) {
+                if (a.outk == OUT_POWER) tpfl_group<EXP, OUT_POWER>(b, g, rows, s_tw1, s_tw2, w4, lane);
+                else tpfl_group<EXP, OUT_POWER_SERIAL>(b, g, rows, s_tw1, s_tw2, w4, lane);
+            }
+            cp_async_wait_all();
+            return;
+        }
+    }
     if constexpr (batch_pair_exp(EXP)) {
         if (a.outk == OUT_POWER && a.tw_pair) {
             // two frames per FFT: pairs f0/2 .. of the tile (f0 and nf are even
