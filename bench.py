@@ -815,8 +815,8 @@ def run_ours(args):
     # accuracy on a slice of frames: float64 FFT of the same samples
     acc = {}
     if rank == 0:
-        nf = 400
         f0 = geo.qt // 3
+        nf = max(1, min(400, geo.qt - f0))
         s0 = f0 * geo.hop
         xs = x[s0:s0 + (nf - 1) * geo.hop + geo.n_window].cpu().numpy()
         got = d_out[f0 * geo.n_window:(f0 + nf) * geo.n_window].cpu().numpy()
