@@ -72,6 +72,7 @@ struct Context {
     std::vector<Slot*> free_slots;
     std::vector<Slot*> all_slots;
     std::map<std::tuple<int, int, int, int>, int> tuned;          // (exp, outk, dense, log2 frames) -> variant
+    std::map<std::pair<uint32_t, int>, int> batch_tuned;          // (window exps present, log2 frames) -> groups per tile
     // uneven batches: the scratch of ocs_batch_device
     std::mutex batch_mu;
     ocs::internal::BatchScratch batch;
@@ -303,7 +304,7 @@ int grid_size(int exp, int outk, int variant, uint64_t frames)
     int occ;
     {
         std::lock_guard<std::mutex> lk(c.mu);
-        auto key = std::make_pair(exp, outk * 4 + variant);
+        auto key = std::make_pair(exp, outk * VAR_COUNT + variant);
         auto it = c.occupancy.find(key);
         if (it == c.occupancy.end()) {
             occ = std::max(1, variant == VAR_PAIR     ? ocs::pair_occupancy(exp, outk)
@@ -785,18 +786,45 @@ int batch_build(ocs_request* reqs, int count, BatchPlan& bp, bool write_status)
         a.cs = ((r.geo.hop % 4 == 0) && (reinterpret_cast<uintptr_t>(q.in) & 15u) == 0) ? 16 : (a.vec2 ? 8 : 4);
         a.exp = r.exp;
         a.outk = outk_of(i);
-        const uint32_t idx = (uint32_t)bp.descs.size();
         bp.descs.push_back(a);
-        const uint64_t tf = (uint64_t)ocs::batch_tile_frames(r.exp);
-        for (uint64_t f0 = 0; f0 < r.geo.frames; f0 += tf) {
+    }
+    return OCS_OK;
+}
+
+// Tile lengths the batch autotuner tries, in CTA-groups of frames per tile:
+// longer tiles mean fewer queue pulls and block barriers, shorter ones a
+// shorter tail.  16 is the default (measured best on average over mixes).
+constexpr int kBatchGroups[] = {8, 16, 32, 64};
+constexpr int kBatchGroupsDefault = 16;
+constexpr int kBatchGroupsMin = 8;
+
+// cuts every descriptor's frames into tiles of `groups` CTA-groups
+void batch_tiles(BatchPlan& bp, int groups)
+{
+    bp.tiles.clear();
+    for (uint32_t idx = 0; idx < (uint32_t)bp.descs.size(); ++idx) {
+        const ocs::FusedArgs& a = bp.descs[idx];
+        const uint64_t tf = (uint64_t)ocs::batch_tile_frames(a.exp, groups);
+        for (uint64_t f0 = 0; f0 < a.frames; f0 += tf) {
             ocs::BatchTile t;
             t.req = idx;
-            t.nframes = (uint32_t)std::min<uint64_t>(tf, r.geo.frames - f0);
+            t.nframes = (uint32_t)std::min<uint64_t>(tf, a.frames - f0);
             t.f0 = f0;
             bp.tiles.push_back(t);
         }
     }
-    return OCS_OK;
+}
+
+// the autotuner's key for a batch: which window sizes it holds and its size
+std::pair<uint32_t, int> batch_mix_key(const BatchPlan& bp)
+{
+    uint32_t mask = 0;
+    uint64_t frames = 0;
+    for (const ocs::FusedArgs& a : bp.descs) {
+        mask |= 1u << a.exp;
+        frames += a.frames;
+    }
+    return std::make_pair(mask, ilog2u(frames));
 }
 
 size_t batch_bytes(size_t ndesc, size_t ntiles)
@@ -856,14 +884,86 @@ int batch_prepare_into(const ocs_request* reqs, int count, BatchScratch& b)
     int rc = batch_build(copy.data(), count, bp, true);
     if (rc) return rc;
     batch_occ_get();
+    batch_tiles(bp, kBatchGroupsMin);  // room for the most tiles any tuned length makes
     return batch_scratch_grow(b, batch_bytes(bp.descs.size(), bp.tiles.size()));
 }
+
+namespace {
+
+// Stages bp's descriptors and tiles in b and launches the persistent kernel.
+int batch_launch(const BatchPlan& bp, cudaStream_t st, BatchScratch& b, bool capturing)
+{
+    Context& c = ctx();
+    const size_t bytes = batch_bytes(bp.descs.size(), bp.tiles.size());
+    if (capturing && (b.host_cap < bytes || b.dev_cap < bytes))
+        return fail(OCS_ENOMEM, "batch buffers not prepared (call ocs_batch_prepare before each capture)");
+    int rc = batch_scratch_grow(b, bytes);
+    if (rc) return rc;
+    const int occ = batch_occ_get();
+    if (!capturing) {
+        // the previous batch's descriptors must have left the staging buffer,
+        // and its kernel must be done reading the device copy
+        OCS_CUDA(cudaEventSynchronize(b.staged));
+        OCS_CUDA(cudaStreamWaitEvent(st, b.done, 0));
+    }
+    const size_t o_tiles = align256(bp.descs.size() * sizeof(ocs::FusedArgs));
+    const size_t o_cnt = o_tiles + align256(bp.tiles.size() * sizeof(ocs::BatchTile));
+    std::memcpy(b.host, bp.descs.data(), bp.descs.size() * sizeof(ocs::FusedArgs));
+    std::memcpy(b.host + o_tiles, bp.tiles.data(), bp.tiles.size() * sizeof(ocs::BatchTile));
+    const uint32_t nt = (uint32_t)bp.tiles.size();
+    std::memcpy(b.host + o_cnt, &nt, 4);
+    std::memset(b.host + o_cnt + 4, 0, 4);  // tile counter starts at zero
+    OCS_CUDA(cudaMemcpyAsync(b.dev, b.host, o_cnt + 8, cudaMemcpyHostToDevice, st));
+    if (!capturing) OCS_CUDA(cudaEventRecord(b.staged, st));
+    auto* d_reqs = reinterpret_cast<const ocs::FusedArgs*>(b.dev);
+    auto* d_tiles = reinterpret_cast<const ocs::BatchTile*>(b.dev + o_tiles);
+    auto* d_nt = reinterpret_cast<const uint32_t*>(b.dev + o_cnt);
+    auto* d_cnt = reinterpret_cast<uint32_t*>(b.dev + o_cnt + 4);
+    const int grid = std::max(1, std::min<int>(c.sms * occ, (int)bp.tiles.size()));
+    OCS_CUDA(ocs::launch_batch(d_reqs, d_tiles, d_nt, d_cnt, grid, st));
+    if (!capturing) OCS_CUDA(cudaEventRecord(b.done, st));
+    return OCS_OK;
+}
+
+// Times each tile length on this batch (every run writes the same outputs)
+// and returns the fastest; the caller's launch then writes them once more.
+int batch_tune(BatchPlan& bp, cudaStream_t st, BatchScratch& b, int* best_groups)
+{
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t te = cudaEventCreate(&e0);
+    if (te == cudaSuccess) te = cudaEventCreate(&e1);
+    float best = 1e30f;
+    *best_groups = kBatchGroupsDefault;
+    int rc = OCS_OK;
+    for (int g : kBatchGroups) {
+        if (te != cudaSuccess || rc) break;
+        batch_tiles(bp, g);
+        rc = batch_launch(bp, st, b, false);  // warm-up
+        if (!rc) te = cudaEventRecord(e0, st);
+        for (int k = 0; k < 2 && !rc && te == cudaSuccess; ++k) rc = batch_launch(bp, st, b, false);
+        if (!rc && te == cudaSuccess) te = cudaEventRecord(e1, st);
+        if (!rc && te == cudaSuccess) te = cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        if (!rc && te == cudaSuccess) te = cudaEventElapsedTime(&ms, e0, e1);
+        if (!rc && te == cudaSuccess && ms < best) {
+            best = ms;
+            *best_groups = g;
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (te != cudaSuccess) return cuda_fail(te, "batch tile timing");
+    return OCS_OK;
+}
+
+}  // namespace
 
 // Uploads the descriptors of one batch into `b` and launches the persistent
 // kernel on `st`.  The scratch is reused only after the previous batch that
 // used it has read it (GPU-side wait), so batches on different streams with
 // different scratch objects run concurrently.
-int batch_enqueue(ocs_request* reqs, int count, cudaStream_t st, BatchScratch& b)
+int batch_enqueue(ocs_request* reqs, int count, cudaStream_t st, BatchScratch& b, bool tune)
 {
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     OCS_CUDA(cudaStreamIsCapturing(st, &cap));
@@ -872,35 +972,27 @@ int batch_enqueue(ocs_request* reqs, int count, cudaStream_t st, BatchScratch& b
     int rc = batch_build(reqs, count, bp, true);
     if (rc) return rc;
     Context& c = ctx();
-    if (!bp.tiles.empty()) {
-        const size_t bytes = batch_bytes(bp.descs.size(), bp.tiles.size());
-        if (capturing && (b.host_cap < bytes || b.dev_cap < bytes))
-            return fail(OCS_ENOMEM, "batch buffers not prepared (call ocs_batch_prepare before each capture)");
-        rc = batch_scratch_grow(b, bytes);
-        if (rc) return rc;
-        const int occ = batch_occ_get();
-        if (!capturing) {
-            // the previous batch's descriptors must have left the staging buffer,
-            // and its kernel must be done reading the device copy
-            OCS_CUDA(cudaEventSynchronize(b.staged));
-            OCS_CUDA(cudaStreamWaitEvent(st, b.done, 0));
+    if (!bp.descs.empty()) {
+        const auto key = batch_mix_key(bp);
+        int groups = kBatchGroupsDefault;
+        bool known = false;
+        {
+            std::lock_guard<std::mutex> lk(c.mu);
+            auto it = c.batch_tuned.find(key);
+            if (it != c.batch_tuned.end()) {
+                groups = it->second;
+                known = true;
+            }
         }
-        const size_t o_tiles = align256(bp.descs.size() * sizeof(ocs::FusedArgs));
-        const size_t o_cnt = o_tiles + align256(bp.tiles.size() * sizeof(ocs::BatchTile));
-        std::memcpy(b.host, bp.descs.data(), bp.descs.size() * sizeof(ocs::FusedArgs));
-        std::memcpy(b.host + o_tiles, bp.tiles.data(), bp.tiles.size() * sizeof(ocs::BatchTile));
-        const uint32_t nt = (uint32_t)bp.tiles.size();
-        std::memcpy(b.host + o_cnt, &nt, 4);
-        std::memset(b.host + o_cnt + 4, 0, 4);  // tile counter starts at zero
-        OCS_CUDA(cudaMemcpyAsync(b.dev, b.host, o_cnt + 8, cudaMemcpyHostToDevice, st));
-        if (!capturing) OCS_CUDA(cudaEventRecord(b.staged, st));
-        auto* d_reqs = reinterpret_cast<const ocs::FusedArgs*>(b.dev);
-        auto* d_tiles = reinterpret_cast<const ocs::BatchTile*>(b.dev + o_tiles);
-        auto* d_nt = reinterpret_cast<const uint32_t*>(b.dev + o_cnt);
-        auto* d_cnt = reinterpret_cast<uint32_t*>(b.dev + o_cnt + 4);
-        const int grid = std::max(1, std::min<int>(c.sms * occ, (int)bp.tiles.size()));
-        OCS_CUDA(ocs::launch_batch(d_reqs, d_tiles, d_nt, d_cnt, grid, st));
-        if (!capturing) OCS_CUDA(cudaEventRecord(b.done, st));
+        if (tune && !known && !capturing && !env_is("OCS_AUTOTUNE", "0")) {
+            rc = batch_tune(bp, st, b, &groups);
+            if (rc) return rc;
+            std::lock_guard<std::mutex> lk(c.mu);
+            c.batch_tuned[key] = groups;
+        }
+        batch_tiles(bp, groups);
+        rc = batch_launch(bp, st, b, capturing);
+        if (rc) return rc;
     }
     for (int i : bp.big) {
         const Request& r = bp.parsed[i];
@@ -938,7 +1030,7 @@ extern "C" int ocs_batch_device(ocs_request* reqs, int count, void* stream)
     OCS_CUDA(cudaStreamIsCapturing(st, &cap));
     Context& c = ctx();
     std::lock_guard<std::mutex> lk(c.batch_mu);
-    if (cap == cudaStreamCaptureStatusNone) return ocs::internal::batch_enqueue(reqs, count, st, c.batch);
+    if (cap == cudaStreamCaptureStatusNone) return ocs::internal::batch_enqueue(reqs, count, st, c.batch, true);
     if (!c.graph_next)
         return fail(OCS_ENOMEM, "batch buffers not prepared (call ocs_batch_prepare before each capture)");
     rc = ocs::internal::batch_enqueue(reqs, count, st, *c.graph_next);

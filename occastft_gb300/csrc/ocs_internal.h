@@ -24,7 +24,9 @@ struct BatchScratch {
 int batch_scratch_grow(BatchScratch& b, size_t bytes);
 void batch_scratch_release(BatchScratch& b);
 int batch_prepare_into(const ocs_request* reqs, int count, BatchScratch& b);
-int batch_enqueue(ocs_request* reqs, int count, cudaStream_t st, BatchScratch& b);
+// tune: time the tile lengths on this call when the batch's mix is new
+// (ocs_batch_device outside capture; the server never tunes)
+int batch_enqueue(ocs_request* reqs, int count, cudaStream_t st, BatchScratch& b, bool tune = false);
 int ensure_ready();
 // drops the no-allocation batch's per-device set-up (ocs_shutdown)
 void noalloc_forget_devices();

@@ -84,7 +84,7 @@ struct BatchTile {
     uint64_t f0;       // first frame
 };
 bool batch_supports(int exp);
-int batch_tile_frames(int exp);
+int batch_tile_frames(int exp, int groups);
 int batch_occupancy();
 size_t batch_smem_bytes();
 cudaError_t launch_batch(const FusedArgs* d_reqs, const BatchTile* d_tiles, const uint32_t* d_ntiles,

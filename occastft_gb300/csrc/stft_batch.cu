@@ -274,10 +274,9 @@ stft_batch_kernel(const FusedArgs* __restrict__ reqs, const BatchTile* __restric
 
 size_t batch_smem_bytes() { return batch_smem_ct(); }
 bool batch_supports(int exp) { return exp >= kBatchMinExp && exp <= kBatchMaxExp; }
-// 16 CTA-groups of frames per tile: fewer queue pulls and block barriers
-// (uneven batch: 4 groups 11.66 ms, 8 11.22, 16 11.00, 32 10.93, 64 11.03),
-// while small batches still cut into more tiles than there are CTAs
-int batch_tile_frames(int exp) { return fused_fpc(exp) * 16; }
+// a tile is `groups` CTA-groups of frames (the host's autotuner picks the
+// count per batch mix; any count keeps tiles whole groups of every body)
+int batch_tile_frames(int exp, int groups) { return fused_fpc(exp) * groups; }
 
 int batch_occupancy()
 {

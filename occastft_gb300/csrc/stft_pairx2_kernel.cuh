@@ -37,13 +37,16 @@ namespace ocs {
 constexpr int kPx2Exp = 10;
 constexpr int kPx2Row = 66;                  // floats per row of an exchange plane (64 + 2 padding)
 constexpr int kPx2Plane = 16 * kPx2Row;      // floats per plane (1024 points)
-constexpr int kPx2PPC = 8;                   // frame pairs per 256-thread CTA (one warp each)
+// frame pairs per CTA (one warp each); 9 warps per CTA at 108 registers (18
+// warps per SM against 16) measured no faster: 447-451 against 452 Gsamples/s
+constexpr int kPx2PPC = 8;
+constexpr int kPx2Threads = 32 * kPx2PPC;
 constexpr size_t kPx2Smem = 512 * 16         // stage-2 twiddles, float4 per (pair slot, thread)
                             + 512 * 8        // window pairs
                             + (size_t)kPx2PPC * 2 * kPx2Plane * 4;
 
 template <int OUTK>
-__global__ void __launch_bounds__(256, 2) stft_pairx2_kernel(const FusedArgs a)
+__global__ void __launch_bounds__(kPx2Threads, 2) stft_pairx2_kernel(const FusedArgs a)
 {
     using namespace x2;
     constexpr int N = 1024, H = 512;

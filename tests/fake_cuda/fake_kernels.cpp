@@ -69,7 +69,7 @@ int pair_twiddle_count(int exp) { return 1 << exp; }
 cudaError_t build_pair_twiddles(float2*, int, cudaStream_t) { return no_work(); }
 
 bool batch_supports(int exp) { return exp >= 6 && exp <= 13; }
-int batch_tile_frames(int exp) { return exp <= 9 ? 64 : 16; }
+int batch_tile_frames(int exp, int groups) { return (exp <= 9 ? 4 : 1) * groups; }
 int batch_occupancy() { return 2; }
 size_t batch_smem_bytes() { return 0; }
 cudaError_t launch_batch(const FusedArgs* d_reqs, const BatchTile* d_tiles, const uint32_t* d_ntiles,

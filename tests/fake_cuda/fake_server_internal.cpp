@@ -26,7 +26,7 @@ namespace internal {
 
 // The batch launch: validates each request as the library does and queues one
 // unit of stream work that writes fake::expected() into every output.
-int batch_enqueue(ocs_request* reqs, int count, cudaStream_t st, BatchScratch&)
+int batch_enqueue(ocs_request* reqs, int count, cudaStream_t st, BatchScratch&, bool)
 {
     struct Item {
         const float* in;
