@@ -984,6 +984,14 @@ int batch_enqueue(ocs_request* reqs, int count, cudaStream_t st, BatchScratch& b
                 known = true;
             }
         }
+        // OCS_BATCH_GROUPS=8|16|32|64 fixes the tile length (tests, sweeps)
+        if (const char* eg = std::getenv("OCS_BATCH_GROUPS")) {
+            for (int g : kBatchGroups)
+                if (std::atoi(eg) == g) {
+                    groups = g;
+                    known = true;
+                }
+        }
         if (tune && !known && !capturing && !env_is("OCS_AUTOTUNE", "0")) {
             rc = batch_tune(bp, st, b, &groups);
             if (rc) return rc;

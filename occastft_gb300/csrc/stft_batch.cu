@@ -12,6 +12,13 @@
 
 namespace ocs {
 
+// frames of the next tile a CTA sends toward L2 when it claims that tile
+// (-DOCS_BATCH_CLAIM_PREFETCH builds variant libraries for sweeps)
+#ifndef OCS_BATCH_CLAIM_PREFETCH
+#define OCS_BATCH_CLAIM_PREFETCH 16
+#endif
+constexpr uint32_t kBatchClaimPrefetch = OCS_BATCH_CLAIM_PREFETCH;
+
 constexpr int kBatchMinExp = 6;
 constexpr int kBatchMaxExp = 13;
 
@@ -251,7 +258,7 @@ stft_batch_kernel(const FusedArgs* __restrict__ reqs, const BatchTile* __restric
             if (nx < nt) {
                 const BatchTile tn = tiles[nx];
                 const FusedArgs& an = reqs[tn.req];
-                const uint64_t k = tn.nframes < 16u ? tn.nframes : 16u;
+                const uint64_t k = tn.nframes < kBatchClaimPrefetch ? tn.nframes : kBatchClaimPrefetch;
                 const uint64_t s0 = tn.f0 * an.hop, end = (tn.f0 + k - 1) * an.hop + (1ull << an.exp);
                 prefetch_l2_span(an.x, s0, end < an.n ? end : an.n);
             }

@@ -18,7 +18,16 @@
 namespace ocs {
 
 // ------------------------------------------------------------ plan
-__host__ __device__ constexpr int pair_R(int exp) { return exp <= 6 ? 16 : 32; }
+// -DOCS_PAIR_R16_MASK=(1<<e | ...) (16 values per thread at those windows) and
+// -DOCS_PAIR_MINB_R16 (their kernels' CTAs per SM) build variant libraries
+// for sweeps of the plan
+#ifndef OCS_PAIR_R16_MASK
+#define OCS_PAIR_R16_MASK 0
+#endif
+__host__ __device__ constexpr int pair_R(int exp)
+{
+    return exp <= 6 ? 16 : (((OCS_PAIR_R16_MASK) >> exp) & 1) ? 16 : 32;
+}
 __host__ __device__ constexpr int pair_min_blocks(int exp);
 
 __host__ __device__ constexpr FusedCfg pair_cfg(int exp)
@@ -60,6 +69,9 @@ __host__ __device__ constexpr bool pair_supported(int exp) { return exp >= 6 && 
 // block-wide exchange costs more than the occupancy gains)
 __host__ __device__ constexpr int pair_min_blocks(int exp)
 {
+#ifdef OCS_PAIR_MINB_R16
+    if (((OCS_PAIR_R16_MASK) >> exp) & 1) return OCS_PAIR_MINB_R16;
+#endif
     return pair_cta_threads(exp) >= 512 ? 1 : 512 / pair_cta_threads(exp);
 }
 // Twiddle entries copied to shared memory: the whole table up to 2^11; above,

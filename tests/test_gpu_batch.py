@@ -77,6 +77,28 @@ def test_batch_deterministic(ocs_lib):
         assert np.array_equal(x, y, equal_nan=True)
 
 
+def test_tile_length_changes_nothing(ocs_lib, orc, monkeypatch):
+    """Every tile length the batch autotuner may pick (8 .. 64 frame groups per
+    tile) writes the same bytes: tiles only split frames between CTAs."""
+    items = _mix(40, seed=7, exps=range(6, 14))
+    outs = {}
+    for g in ("8", "16", "32", "64"):
+        monkeypatch.setenv("OCS_BATCH_GROUPS", g)
+        st, out, bufs = _run_batch(ocs_lib, items)
+        assert all(s == 0 for s in st), (g, st)
+        outs[g] = [o[: b[2].out_floats] for o, b in zip(out, bufs)]
+    for g in ("16", "32", "64"):
+        for a, b in zip(outs["8"], outs[g]):
+            assert np.array_equal(a, b), g
+    # and the tuned choice (first uncaptured call of this mix) too
+    monkeypatch.delenv("OCS_BATCH_GROUPS")
+    st, out, bufs = _run_batch(ocs_lib, items)
+    for a, o, b in zip(outs["8"], out, bufs):
+        assert np.array_equal(a, o[: b[2].out_floats])
+    for (x, exp, ov, opts), a in zip(items, outs["8"]):
+        assert orc.rel_l2(a, orc.fp64_stft(x, exp, ov, opts)) <= REL_L2, (exp, ov, opts)
+
+
 def test_per_request_errors(ocs_lib, orc):
     import torch
 
