@@ -297,6 +297,60 @@ __global__ void __launch_bounds__(2 * kTileR * (fused_M(EXP2) / fused_cfg(EXP2).
     // formed once per group.
     const bool dc = a.remove_dc != 0;
     const uint32_t m1 = (uint32_t)M1, m2 = (uint32_t)M2;
+    if constexpr (OUTK == OUT_POWER || OUTK == OUT_POWER_SERIAL) {
+        // Power: one untangle at k gives X[k] and X[M + k], and for a real
+        // frame |X[N - k]| = |X[k]|, |X[M - k]| = |X[M + k]|, so only the 8
+        // rows are untangled and their mirrors (which hold the partners)
+        // come for free.  Row 0 pairs with itself (k2 with M2 - k2) and so
+        // does row M1/2 (k2 with M2 - 1 - k2): the first CTA's slot 0 takes
+        // row 0 for k2 < M2/2, row M1/2 for the other half, and k = M/2 last.
+        const int s = tid & (kTileR - 1);
+        const bool special = b == 0 && s == 0;
+        const uint32_t k1 = (uint32_t)row_of(s);
+        const float2* zs = sbuf + s * BS + large_row_shift(s);
+        const float2* zp = sbuf + (s + kTileR) * BS + large_row_shift(s + kTileR);
+        const float2 wk1 = special ? tw2l(a.twn_lo, a.twn_hi, m1 / 2) : tw2l(a.twn_lo, a.twn_hi, k1);
+        float* ro = a.out + f * (a.dense ? M + 1 : N);
+        auto emit = [&](uint32_t k, float2 A, float2 B, float2 w) {
+            float2 ev, wo;
+            K::untangle(A, B, w, ev, wo);
+            float2 X0 = make_float2(ev.x + wo.x, ev.y + wo.y);        // X[k]
+            const float2 X1 = make_float2(ev.x - wo.x, ev.y - wo.y);  // X[k + M]
+            if (dc && k == 0) X0 = make_float2(0.0f, 0.0f);
+            const float p0 = power_of<OUTK>(X0), p1 = power_of<OUTK>(X1);
+            const bool mirror = k != 0 && k != (uint32_t)(M / 2);
+            if (!a.dense) {
+                __stcs(ro + k, p0);
+                __stcs(ro + (k + M), p1);
+                if (mirror) {
+                    __stcs(ro + (N - k), p0);
+                    __stcs(ro + (M - k), p1);
+                }
+            } else {
+                __stcs(ro + k, p0);
+                if (mirror) __stcs(ro + (M - k), p1);
+                if (k == 0) __stcs(ro + M, p1);
+            }
+        };
+        if (!special) {
+#pragma unroll 2
+            for (uint32_t k2 = (uint32_t)tid / kTileR; k2 < m2; k2 += blockDim.x / kTileR)
+                emit(k1 + m1 * k2, zs[K::pd((int)k2)], zp[K::pd((int)(m2 - 1 - k2))], cmul(wk1, a.tw2[k2]));
+        } else {
+            for (uint32_t k2 = (uint32_t)tid / kTileR; k2 < m2; k2 += blockDim.x / kTileR) {
+                if (k2 < m2 / 2) {
+                    emit(m1 * k2, zs[K::pd((int)k2)], zs[K::pd((int)((m2 - k2) & (m2 - 1)))], a.tw2[k2]);
+                } else {
+                    const uint32_t hk = k2 - m2 / 2;  // row M1/2 sits in slot kTileR
+                    emit(m1 / 2 + m1 * hk, zp[K::pd((int)hk)], zp[K::pd((int)(m2 - 1 - hk))], cmul(wk1, a.tw2[hk]));
+                }
+            }
+            if (tid == 0) {
+                const float2 A = zs[K::pd((int)(m2 / 2))];
+                emit((uint32_t)(M / 2), A, A, a.tw2[m2 / 2]);
+            }
+        }
+    } else {
 #pragma unroll 1
     for (int h = 0; h < 2; ++h) {
         const int s = (tid & (kTileR - 1)) + kTileR * h;
@@ -349,6 +403,7 @@ __global__ void __launch_bounds__(2 * kTileR * (fused_M(EXP2) / fused_cfg(EXP2).
                 }
             }
         }
+    }
     }
 }
 
