@@ -93,6 +93,19 @@ int ocs_activate(const float* in, uint64_t n, int window_size_exp, float overlap
 int ocs_activate_device(const float* d_in, uint64_t n, int window_size_exp, float overlap_ratio,
                         const char* options, float* d_out, uint64_t out_cap, void* stream);
 
+/* Plan tuning ahead of the first request (new; the reference has no
+ * counterpart).  Times the kernel variants that apply to requests of this
+ * shape (window size, output kind and layout, and the size class of the
+ * frame count, for the whole request and for one chunk of ocs_activate's
+ * copy/compute pipeline) on scratch buffers of that size, and keeps the
+ * fastest, as the first call of that shape would.  *variant (may be NULL)
+ * receives the variant the whole request runs: 0 one frame per FFT, 1 the
+ * same with staged I/O, 2 two frames per FFT, 3 lanes per frame, 4 two
+ * frames per FFT on packed FP32x2; -1 where the shape has one form (windows
+ * above 2^15, tensor-core precisions).  With OCS_AUTOTUNE=0 nothing is timed
+ * and the default variant is reported.  Synchronous. */
+int ocs_plan_tune(uint64_t n, int window_size_exp, float overlap_ratio, const char* options, int* variant);
+
 /* The window coefficients the runner applies (host computation, no device
  * needed): the reference's formulas (OKL/kernel.okl:33-127) evaluated with
  * the same float/double roundings as its Serial runner, so they match that

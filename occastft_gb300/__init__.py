@@ -84,6 +84,7 @@ SIGNATURES = {
     "ocs_activate_device": (ctypes.c_int, [_VP, ctypes.c_uint64, ctypes.c_int, ctypes.c_float, ctypes.c_char_p,
                                            _VP, ctypes.c_uint64, _VP]),
     "ocs_window_table": (ctypes.c_int, [ctypes.c_int, ctypes.c_uint32, ctypes.c_float, _VP]),
+    "ocs_plan_tune": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_int, ctypes.c_float, ctypes.c_char_p, _VP]),
     "ocs_host_alloc": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t]),
     "ocs_host_free": (ctypes.c_int, [_VP]),
     "ocs_host_register": (ctypes.c_int, [_VP, ctypes.c_size_t]),
@@ -196,6 +197,14 @@ def activate_device(d_in, n: int, window_size_exp: int, overlap_ratio: float, op
     pout = _device_ptr(d_out, out_cap, "output")
     _check(lib().ocs_activate_device(pin, n, window_size_exp, overlap_ratio, options.encode(), pout, out_cap,
                                      _stream_handle(stream)))
+
+
+def plan_tune(n: int, window_size_exp: int, overlap_ratio: float, options: str) -> int:
+    """Tune the kernel choice for requests of this shape ahead of the first one;
+    returns the chosen variant (-1 where the shape has a single form)."""
+    v = ctypes.c_int(-1)
+    _check(lib().ocs_plan_tune(n, window_size_exp, overlap_ratio, options.encode(), ctypes.byref(v)))
+    return v.value
 
 
 def window_table(kind: int, window_size: int, sigma: float = -1.0) -> np.ndarray:

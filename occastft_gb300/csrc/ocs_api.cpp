@@ -350,9 +350,13 @@ int prepare(uint64_t n, int exp, float ov, const char* options, Request& r)
     return OCS_OK;
 }
 
+// the variant this thread launched last (ocs_plan_tune reports it)
+thread_local int g_last_variant = -1;
+
 cudaError_t launch_variant(int v, const Request& r, int outk, ocs::FusedArgs a, const float2* tw_single,
                            const float2* tw_pair, cudaStream_t st)
 {
+    g_last_variant = v;
     if (v == VAR_PAIR) {
         a.tw = tw_pair;
         return ocs::launch_pair(r.exp, outk, a, grid_size(r.exp, outk, VAR_PAIR, a.frames), st);
@@ -1228,6 +1232,49 @@ int ocs_activate(const float* in, uint64_t n, int exp, float ov, const char* opt
         if (rc) return rc;
     }
     if (out_len) *out_len = r.geo.out_floats;
+    return OCS_OK;
+}
+
+int ocs_plan_tune(uint64_t n, int exp, float ov, const char* options, int* variant)
+{
+    if (variant) *variant = -1;
+    Request r;
+    int rc = prepare(n, exp, ov, options, r);
+    if (rc) return rc;
+    rc = ensure_init();
+    if (rc) return rc;
+    // windows above the fused kernels and the tensor-core precisions have one form each
+    if (ocs::large_supports(r.exp) || r.opt.precision >= 1) return OCS_OK;
+    const uint64_t N = r.geo.n_window, hop = r.geo.hop, F = r.geo.frames;
+    const uint64_t need_in = std::max<uint64_t>(1, std::min<uint64_t>(n, (F - 1) * hop + N));
+    const uint64_t need_out = std::max<uint64_t>(1, r.geo.out_floats);
+    Context& c = ctx();
+    float* d_in = nullptr;
+    float* d_out = nullptr;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&d_in), need_in * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&d_out), need_out * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_in, 0, need_in * sizeof(float), c.s_setup);
+    if (e != cudaSuccess) {
+        if (d_in) cudaFree(d_in);
+        if (d_out) cudaFree(d_out);
+        return cuda_fail(e, "plan tuning buffers");
+    }
+    // the whole request (ocs_activate_device) and one chunk of ocs_activate's
+    // copy/compute pipeline: the tuner keys on the frame count's size class
+    rc = launch_frames(r, d_in, need_in, d_out, 0, F, c.s_setup);
+    const int chosen = g_last_variant;
+    if (!rc) {
+        const uint64_t target = std::max<uint64_t>(1, (8ull << 20) / 4 / std::max<uint64_t>(hop, 1));
+        const uint64_t chunks = std::min<uint64_t>(kMaxChunks, std::max<uint64_t>(1, (F + target - 1) / target));
+        const uint64_t per = (F + chunks - 1) / chunks;
+        if (per < F) rc = launch_frames(r, d_in, need_in, d_out, 0, per, c.s_setup);
+    }
+    const cudaError_t es = cudaStreamSynchronize(c.s_setup);
+    cudaFree(d_in);
+    cudaFree(d_out);
+    if (rc) return rc;
+    if (es != cudaSuccess) return cuda_fail(es, "plan tuning");
+    if (variant) *variant = chosen;
     return OCS_OK;
 }
 

@@ -397,6 +397,39 @@ void capture_tune()
     std::printf("ok %s\n", name);
 }
 
+void plan_tune()
+{
+    const char* name = "plan_tune";
+    setenv("OCS_AUTOTUNE", "1", 1);
+    int v = -7;
+    // a key not tuned before: the call times the variants and reports the choice
+    check(ocs_plan_tune(3000000, 10, 0.5f, "--blackman_window --remove_dc", &v) == OCS_OK, name, "tune");
+    check(v >= 0 && v <= 4, name, "variant " + std::to_string(v));
+    // again (the plan's tables are cached by now): the same choice, no scratch kept
+    const long allocs0 = fake::live_allocs.load();
+    int v2 = -7;
+    check(ocs_plan_tune(3000000, 10, 0.5f, "--blackman_window --remove_dc", &v2) == OCS_OK && v2 == v, name,
+          "second call");
+    check(fake::live_allocs.load() == allocs0, name, "scratch left behind");
+    // the tuned request then runs with that choice and the expected result
+    std::vector<float> x = make_signal(3000000, 5);
+    ocs_geometry g;
+    check(ocs_geometry_get(x.size(), 10, 0.5f, "--blackman_window --remove_dc", &g) == OCS_OK, name, "geometry");
+    std::vector<float> out(g.out_floats);
+    uint64_t len = 0;
+    check(ocs_activate(x.data(), x.size(), 10, 0.5f, "--blackman_window --remove_dc", out.data(), out.size(), &len) ==
+              OCS_OK,
+          name, "activate");
+    check(std::memcmp(out.data(), expected_out(x.data(), x.size(), 10, 0.5f, "--blackman_window --remove_dc").data(),
+                      out.size() * 4) == 0,
+          name, "result");
+    // one form only: windows above 2^15; and the option errors of ocs_activate
+    check(ocs_plan_tune(1 << 20, 16, 0.5f, "--hamming_window", &v) == OCS_OK && v == -1, name, "large window");
+    check(ocs_plan_tune(1 << 20, 10, 1.5f, "--hamming_window", &v) == OCS_EINVAL && v == -1, name, "bad overlap");
+    setenv("OCS_AUTOTUNE", "0", 1);
+    std::printf("ok %s\n", name);
+}
+
 void shutdown()
 {
     const char* name = "shutdown";
@@ -465,6 +498,7 @@ int main(int argc, char** argv)
     slot_fail();
     tune_fail();
     capture_tune();  // before any check that tunes other keys
+    plan_tune();
     activate();
     concurrent();
     batch();

@@ -66,6 +66,7 @@ cudaError_t cudaEventRecord(cudaEvent_t ev, cudaStream_t st);
 cudaError_t cudaEventSynchronize(cudaEvent_t ev);
 cudaError_t cudaEventElapsedTime(float* ms, cudaEvent_t start, cudaEvent_t end);
 cudaError_t cudaMemcpyAsync(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t st);
+cudaError_t cudaMemsetAsync(void* dst, int value, size_t bytes, cudaStream_t st);
 cudaError_t cudaLaunchHostFunc(cudaStream_t st, cudaHostFn_t fn, void* arg);
 cudaError_t cudaGetLastError(void);
 const char* cudaGetErrorString(cudaError_t e);

@@ -303,6 +303,11 @@ cudaError_t cudaEventElapsedTime(float* ms, cudaEvent_t start, cudaEvent_t end)
     *ms = (float)std::max(0.0, end->t_ms - start->t_ms);
     return cudaSuccess;
 }
+cudaError_t cudaMemsetAsync(void* dst, int value, size_t bytes, cudaStream_t st)
+{
+    stream_of(st)->push([dst, value, bytes] { std::memset(dst, value, bytes); });
+    return cudaSuccess;
+}
 cudaError_t cudaMemcpyAsync(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t st)
 {
     const void* bad = fake::fail_copy_ptr.load();

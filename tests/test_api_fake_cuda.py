@@ -11,6 +11,7 @@ Covers what the GPU tests cannot make happen on purpose or often enough:
   every stream and slow input copies, with the result written over the
   signal in three placements;
 - four threads calling ocs_activate at once;
+- ocs_plan_tune ahead of a request (its scratch released, the choice kept);
 - uneven batches, the per-capture descriptor buffers, and a full release at
   ocs_shutdown."""
 import os
@@ -25,8 +26,8 @@ CSRC = os.path.join(ROOT, "occastft_gb300", "csrc")
 SOURCES = [os.path.join(CSRC, "ocs_api.cpp"), os.path.join(CSRC, "ocs_host.cpp"),
            os.path.join(FAKE, "fake_runtime.cpp"), os.path.join(FAKE, "fake_kernels.cpp"),
            os.path.join(FAKE, "api_stress.cpp")]
-CHECKS = ["setup_fail", "table_fail", "slot_fail", "tune_fail", "capture_tune", "activate", "concurrent", "batch",
-          "capture", "shutdown"]
+CHECKS = ["setup_fail", "table_fail", "slot_fail", "tune_fail", "capture_tune", "plan_tune", "activate",
+          "concurrent", "batch", "capture", "shutdown"]
 
 
 def _build(out, sanitize):

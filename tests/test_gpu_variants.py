@@ -53,3 +53,22 @@ def test_variant_parity(env):
     for exp, opts, err, size_ok in res:
         assert size_ok, (exp, opts)
         assert err <= 1e-5, (env, exp, opts, err)
+
+
+def test_plan_tune_ahead_of_first_request(ocs_lib, orc):
+    """ocs_plan_tune times the variants for a request shape ahead of time and
+    reports the one the request then runs; the request's result is unchanged."""
+    import numpy as np
+
+    from tests.conftest import signal
+
+    x = signal(4242, 3_000_017)
+    for exp, opts in ((10, "--hamming_window"), (8, "--blackman_window --remove_dc"),
+                      (12, "--hanning_window --half_complex_return"), (9, "--nuttall_window --layout=dense")):
+        v = ocs_lib.plan_tune(x.size, exp, 0.5, opts)
+        assert 0 <= v <= 4, (exp, opts, v)
+        assert ocs_lib.plan_tune(x.size, exp, 0.5, opts) == v  # a tuned key keeps its choice
+        got = ocs_lib.activate(x, exp, 0.5, opts)
+        assert orc.rel_l2(got, orc.fp64_stft(x, exp, 0.5, opts)) <= 1e-5, (exp, opts)
+    assert ocs_lib.plan_tune(x.size, 16, 0.5, "--hamming_window") == -1
+    assert ocs_lib.plan_tune(x.size, 10, 0.75, "--hanning_window --precision=tc-fp16") == -1
