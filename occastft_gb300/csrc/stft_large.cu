@@ -11,8 +11,9 @@
 // X[k + M] = (Z[k] + conj Z[M-k]) - W_N^k (...) (the window table carries the
 // untangle's factor 1/2).
 //
-// Column pass: a CTA owns 8 consecutive columns of one frame.  It reads the
-// frame's samples row by row (64 contiguous bytes per row), applies the
+// Column pass: a CTA owns 16 (windows 2^16, 2^17) or 8 consecutive columns
+// of one frame.  It reads the frame's samples row by row (128 or 64
+// contiguous bytes per row), applies the
 // window, runs 8 M1-point FFTs with the fused kernels' Stockham core, applies
 // W_M^{c k1} and writes Y row-major to a scratch area (again 64-byte rows).
 // Row pass: a CTA owns 8 rows k1 and their 8 mirror rows M1 - k1 (row M1/2
@@ -39,7 +40,7 @@
 namespace ocs {
 namespace {
 
-constexpr int kTileC = 8;  // columns per column-pass CTA
+constexpr int kTileC = 8;  // columns per middle-pass CTA (column pass: large_col_tile)
 constexpr int kTileR = 8;  // rows (and as many mirror rows) per row-pass CTA
 
 // Column-pass buffer stride: = 2 (mod 8) float2.  An 8-byte shared access is
@@ -73,10 +74,26 @@ __device__ __forceinline__ float2 tw2l(const float2* lo, const float2* hi, uint6
 // window coefficients in registers and take 4 consecutive frames of the same
 // columns per CTA; the larger ones (more chunks per thread, or 1024 threads
 // at 64 registers) take one frame per CTA and read the window each time.
+//
+// A CTA owns 16 columns (rows of 128 bytes, 8 lanes per row) where that keeps
+// it at 256 threads (column FFTs of 256 points, windows 2^16 and 2^17), else
+// 8: each warp-wide row load then touches half as many cache lines.
+__host__ __device__ constexpr int large_col_tile(int exp1)
+{
+    return 16 * (fused_M(exp1) / fused_cfg(exp1).R) <= 256 ? 16 : 8;
+}
+// Its buffer stride: with 16 columns an odd number of float2, so that a
+// half-warp's 8-byte staging accesses (2 rows x 8 lanes, lane q on columns 2q
+// and 2q + 1) land on 16 distinct bank pairs; with 8 columns the stride of
+// the middle pass.
+__host__ __device__ constexpr int large_col_stride_t(int exp1, int tc)
+{
+    return tc == 16 ? (fused_buf_stride(exp1) | 1) : large_col_stride(exp1);
+}
 __host__ __device__ constexpr bool large_col_cache_win(int exp1)
 {
-    return (fused_M(exp1) * 4 / (8 * (fused_M(exp1) / fused_cfg(exp1).R))) <= 8 &&
-           8 * (fused_M(exp1) / fused_cfg(exp1).R) <= 256;
+    return fused_M(exp1) / (2 * (fused_M(exp1) / fused_cfg(exp1).R)) <= 8 &&
+           large_col_tile(exp1) * (fused_M(exp1) / fused_cfg(exp1).R) <= 256;
 }
 __host__ __device__ constexpr int large_col_frames(int exp1) { return large_col_cache_win(exp1) ? 4 : 1; }
 
@@ -87,24 +104,26 @@ __device__ __forceinline__ float4 large_win4(const float* win, uint32_t i)
 }
 
 template <int EXP1>
-__global__ void __launch_bounds__(kTileC * (fused_M(EXP1) / fused_cfg(EXP1).R))
+__global__ void __launch_bounds__(large_col_tile(EXP1) * (fused_M(EXP1) / fused_cfg(EXP1).R))
     large_columns_kernel(const LargeArgs a)
 {
     using K = Core<EXP1>;
     constexpr int M1 = K::M, R = K::R, T = K::T;
-    constexpr int NT = kTileC * T;      // threads
-    constexpr int NE = M1 * 4 / NT;     // float4 row chunks per thread (= R / 2)
-    constexpr int BS = large_col_stride(EXP1);
-    extern __shared__ float2 sbuf[];  // kTileC column buffers of BS slots
+    constexpr int TC = large_col_tile(EXP1);  // columns
+    constexpr int QR = TC / 2;                // float4 chunks per row
+    constexpr int NT = TC * T;                // threads
+    constexpr int NE = M1 * QR / NT;          // float4 row chunks per thread (= R / 2)
+    constexpr int BS = large_col_stride_t(EXP1, TC);
+    extern __shared__ float2 sbuf[];  // TC column buffers of BS slots
     const int tid = threadIdx.x;
     const uint64_t M2 = a.m2;
-    const uint64_t tiles = M2 / kTileC;
+    const uint64_t tiles = M2 / TC;
     const uint64_t fg = blockIdx.x / tiles;  // group of FPC frames within this launch
-    const uint64_t c0 = (blockIdx.x % tiles) * kTileC;
+    const uint64_t c0 = (blockIdx.x % tiles) * TC;
     const uint64_t N = 2 * (uint64_t)M1 * M2;
     const bool aligned = (a.hop & 3) == 0 && (reinterpret_cast<uintptr_t>(a.x) & 15) == 0;
-    // this CTA's window coefficients: chunk j is row m1 = e / 4, columns 2q,
-    // 2q+1 (q = e % 4) with e = tid + j NT; row m1 starts at real index
+    // this CTA's window coefficients: chunk j is row m1 = e / QR, columns 2q,
+    // 2q+1 (q = e % QR) with e = tid + j NT; row m1 starts at real index
     // 2 (c0 + M2 m1), a multiple of 16
     constexpr bool CACHE_WIN = large_col_cache_win(EXP1);
     constexpr int FPC = large_col_frames(EXP1);
@@ -112,7 +131,7 @@ __global__ void __launch_bounds__(kTileC * (fused_M(EXP1) / fused_cfg(EXP1).R))
     if constexpr (CACHE_WIN) {
 #pragma unroll
         for (int j = 0; j < NE; ++j) {
-            const int e = tid + j * NT, m1 = e >> 2, q = e & 3;
+            const int e = tid + j * NT, m1 = e / QR, q = e % QR;
             wv[j] = large_win4(a.win, 2u * ((uint32_t)c0 + (uint32_t)M2 * (uint32_t)m1) + 4u * (uint32_t)q);
         }
     }
@@ -127,13 +146,13 @@ __global__ void __launch_bounds__(kTileC * (fused_M(EXP1) / fused_cfg(EXP1).R))
         const uint64_t f = a.f0 + fl;
         const uint64_t s0 = f * a.hop;
         if (ff > 0) __syncthreads();  // the previous frame's reads of the buffers are over
-        // rows of 8 complex samples (16 floats, 64 bytes)
+        // rows of TC complex samples (64 or 128 bytes)
         if (aligned && f < a.frames_total && s0 + N <= a.n) {
-            // frame inside the signal and 16-byte aligned: four threads per
+            // frame inside the signal and 16-byte aligned: QR threads per
             // row, a float4 (two complex samples) each
             const float* xf = a.x + s0;
             auto chunk = [&](int e, const float4& w) {
-                const int m1 = e >> 2, q = e & 3;
+                const int m1 = e / QR, q = e % QR;
                 const uint32_t i = 2u * ((uint32_t)c0 + (uint32_t)M2 * (uint32_t)m1) + 4u * (uint32_t)q;
                 const float4 xv = *reinterpret_cast<const float4*>(xf + i);
                 sbuf[(2 * q) * BS + K::pd(m1)] = make_float2(xv.x * w.x, xv.y * w.y);
@@ -143,15 +162,15 @@ __global__ void __launch_bounds__(kTileC * (fused_M(EXP1) / fused_cfg(EXP1).R))
 #pragma unroll
                 for (int j = 0; j < NE; ++j) chunk(tid + j * NT, wv[j]);
             } else {
-                for (int e = tid; e < M1 * 4; e += NT) {
-                    const uint32_t i = 2u * ((uint32_t)c0 + (uint32_t)M2 * (uint32_t)(e >> 2)) + 4u * (uint32_t)(e & 3);
+                for (int e = tid; e < M1 * QR; e += NT) {
+                    const uint32_t i = 2u * ((uint32_t)c0 + (uint32_t)M2 * (uint32_t)(e / QR)) + 4u * (uint32_t)(e % QR);
                     chunk(e, large_win4(a.win, i));
                 }
             }
         } else {
             // lane pairs take one row, samples past the signal end read as zero
-            for (int e = tid; e < M1 * kTileC; e += NT) {
-                const int cc = e % kTileC, m1 = e / kTileC;
+            for (int e = tid; e < M1 * TC; e += NT) {
+                const int cc = e % TC, m1 = e / TC;
                 const uint64_t m = c0 + cc + M2 * (uint64_t)m1;  // complex index in the frame
                 const uint64_t i = 2 * m;                         // real sample index in the frame
                 const uint64_t g = s0 + i;
@@ -182,11 +201,11 @@ __global__ void __launch_bounds__(kTileC * (fused_M(EXP1) / fused_cfg(EXP1).R))
             buf[K::pd(k1)] = cmul(v[u], w);
         }
         __syncthreads();
-        // Y row-major: row k1 holds this CTA's 8 columns at c0 (64 bytes),
-        // written as four float4 (two complex values) per row
+        // Y row-major: row k1 holds this CTA's TC columns at c0 (64 or 128
+        // bytes), written as QR float4 (two complex values) per row
         float2* y = a.scratch + fl * (uint64_t)M1 * M2;
-        for (int e = tid; e < M1 * 4; e += NT) {
-            const int k1 = e >> 2, q = e & 3;
+        for (int e = tid; e < M1 * QR; e += NT) {
+            const int k1 = e / QR, q = e % QR;
             const float2 lo = sbuf[(2 * q) * BS + K::pd(k1)], hi = sbuf[(2 * q + 1) * BS + K::pd(k1)];
             *reinterpret_cast<float4*>(y + (uint64_t)k1 * M2 + c0 + 2 * q) = make_float4(lo.x, lo.y, hi.x, hi.y);
         }
@@ -424,15 +443,16 @@ template <int EXP1>
 cudaError_t launch_columns_t(const LargeArgs& a, uint64_t frames, cudaStream_t st)
 {
     constexpr int T = fused_M(EXP1) / fused_cfg(EXP1).R;
-    constexpr size_t smem = (size_t)kTileC * large_col_stride(EXP1) * sizeof(float2);
+    constexpr int TC = large_col_tile(EXP1);
+    constexpr size_t smem = (size_t)TC * large_col_stride_t(EXP1, TC) * sizeof(float2);
     auto k = large_columns_kernel<EXP1>;
     const cudaError_t e = ensure_smem_attr<large_columns_kernel<EXP1>>(smem);
     if (e != cudaSuccess) return e;
     constexpr int FPC = large_col_frames(EXP1);
-    const uint64_t grid = (frames + FPC - 1) / FPC * (a.m2 / kTileC);
+    const uint64_t grid = (frames + FPC - 1) / FPC * (a.m2 / TC);
     LargeArgs b = a;
     b.frames_launch = frames;
-    k<<<(unsigned)grid, kTileC * T, smem, st>>>(b);
+    k<<<(unsigned)grid, TC * T, smem, st>>>(b);
     return cudaGetLastError();
 }
 
