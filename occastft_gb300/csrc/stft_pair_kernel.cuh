@@ -352,6 +352,14 @@ __device__ __forceinline__ void pair_group(const FusedArgs& a, uint64_t pbase, f
                 for (int u = R / 2; u < R; ++u) v[u].y = xb[t + u * T];
 #pragma unroll
                 for (int u = 0; u < R / 2; ++u) v[u].y = v[u + R / 2].x;
+            } else if (EXP <= 12 && act_b && sb + N <= a.n && a.hop == (uint64_t)(N / 4)) {
+                // overlap 0.75: frame b's slots u < 3R/4 are frame a's slots u + R/4
+#pragma unroll
+                for (int u = 0; u < R; ++u) v[u].x = xa[t + u * T];
+#pragma unroll
+                for (int u = 3 * R / 4; u < R; ++u) v[u].y = xb[t + u * T];
+#pragma unroll
+                for (int u = 0; u < 3 * R / 4; ++u) v[u].y = v[u + R / 4].x;
             } else if (act_b && sb + N <= a.n) {
 #pragma unroll
                 for (int u = 0; u < R; ++u) {

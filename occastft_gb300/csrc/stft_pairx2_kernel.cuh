@@ -96,6 +96,13 @@ __global__ void __launch_bounds__(kPx2Threads, 2) stft_pairx2_kernel(const Fused
                     v[j].re = make_float2(xa[t + 32 * j], xa[t + 32 * j + H]);
                     v[j].im = make_float2(v[j].re.y, xb[t + 32 * j + H]);
                 }
+            } else if (act_b && sb + N <= a.n && a.hop == (uint64_t)(N / 4)) {
+                // overlap 0.75: frame b's sample t + 32 j is frame a's t + 32 (j + 8)
+#pragma unroll
+                for (int j = 0; j < 16; ++j) v[j].re = make_float2(xa[t + 32 * j], xa[t + 32 * j + H]);
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                    v[j].im = j < 8 ? v[j + 8].re : make_float2(v[j - 8].re.y, xb[t + 32 * j + H]);
             } else if (act_b && sb + N <= a.n) {
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
