@@ -156,7 +156,11 @@ int ocs_batch_prepare(const ocs_request* reqs, int count);
  * aside (OCS_ENOMEM if there are none, or they are too small) and keeps them
  * until ocs_shutdown, so the graph replays its own requests whatever batches
  * run after the capture.  Replays of one graph must not overlap each other on
- * the GPU (they share those buffers); replays and other batches may. */
+ * the GPU (they share those buffers); replays and other batches may.
+ * The first call outside capture for a new mix of window sizes and batch
+ * size times the tile lengths (8 .. 64 frame groups per tile) on these
+ * requests, running the batch about a dozen times, and waits for that; the
+ * outputs are the same for every length.  OCS_AUTOTUNE=0 skips this. */
 int ocs_batch_device(ocs_request* reqs, int count, void* stream);
 
 /* Same as ocs_batch_device, for callers that must not allocate GPU memory
