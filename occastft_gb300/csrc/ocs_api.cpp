@@ -156,6 +156,7 @@ int ensure_init()
     return init_locked(c, c.ready ? c.device : -1);
 }
 
+// exp: the window exponent, or the plan id of a paired table
 int get_twiddles(int exp, bool paired, const float2** out)
 {
     Context& c = ctx();
@@ -490,7 +491,8 @@ int launch_frames(const Request& r, const float* d_sig, uint64_t n, float* d_out
     int rc = get_twiddles(r.exp, false, &tw_single);
     if (rc) return rc;
     if (ocs::pair_has(r.exp)) {
-        rc = get_twiddles(r.exp, true, &tw_pair);
+        // the one-request kernels' paired plan (the batch's may differ)
+        rc = get_twiddles(ocs::pair_plan_id(r.exp), true, &tw_pair);
         if (rc) return rc;
     }
     rc = get_window(r.opt.window, r.exp, r.opt.sigma, true, &win);

@@ -67,8 +67,11 @@ bool pair_has(int exp);
 cudaError_t launch_pair(int exp, int outk, const FusedArgs& a, int grid, cudaStream_t st);
 int pair_occupancy(int exp, int outk);
 int pair_per_cta(int exp);
-int pair_twiddle_count(int exp);
-cudaError_t build_pair_twiddles(float2* tw, int exp, cudaStream_t st);
+// paired plans are named by an id: the window exponent, with a flag for the
+// one-request kernel's own plan where it differs from the batch's (2^12)
+int pair_plan_id(int exp);
+int pair_twiddle_count(int pid);
+cudaError_t build_pair_twiddles(float2* tw, int pid, cudaStream_t st);
 
 // paired-frame STFT on packed FP32x2 arithmetic (window 2^10): same plan
 // table (a.tw = the pair plan's), one warp per frame pair, 8 pairs per CTA

@@ -42,7 +42,7 @@ __global__ void build_twiddles_kernel(float2* tw, int exp)
     tw[idx] = make_float2((float)cs, (float)(-sn));
 }
 
-// paired-frame tables: stage twiddles only
+// paired-frame tables (of a plan id): stage twiddles only
 __global__ void build_pair_twiddles_kernel(float2* tw, int exp)
 {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -80,13 +80,14 @@ int pair_occupancy(int exp, int outk)
 }
 
 bool pair_has(int exp) { return pair_supported(exp); }
-int pair_per_cta(int exp) { return pair_ppc(exp); }
-int pair_twiddle_count(int exp) { return pair_tw_size(exp); }
+int pair_plan_id(int exp) { return exp == 12 ? (12 | kPairR16) : exp; }
+int pair_per_cta(int exp) { return pair_ppc(pair_plan_id(exp)); }
+int pair_twiddle_count(int pid) { return pair_tw_size(pid); }
 
-cudaError_t build_pair_twiddles(float2* tw, int exp, cudaStream_t st)
+cudaError_t build_pair_twiddles(float2* tw, int pid, cudaStream_t st)
 {
-    const int n = pair_tw_size(exp);
-    build_pair_twiddles_kernel<<<(n + 255) / 256, 256, 0, st>>>(tw, exp);
+    const int n = pair_tw_size(pid);
+    build_pair_twiddles_kernel<<<(n + 255) / 256, 256, 0, st>>>(tw, pid);
     return cudaGetLastError();
 }
 

@@ -18,97 +18,114 @@
 namespace ocs {
 
 // ------------------------------------------------------------ plan
-// -DOCS_PAIR_R16_MASK=(1<<e | ...) (16 values per thread at those windows) and
-// -DOCS_PAIR_MINB_R16 (their kernels' CTAs per SM) build variant libraries
-// for sweeps of the plan
+// A paired plan is named by an id: the window exponent, plus kPairR16 for the
+// variant with 16 values per thread.  The one-request kernel at 2^12 runs that
+// variant (a 16 . 16 . 16 plan at three CTAs per SM, 80 registers: power 305
+// -> 316, half-complex 451 -> 485 Gsamples/s against 32 . 32 . 4); the batch
+// keeps 32 values per thread there (its kernel stays at two CTAs per SM, and
+// its 2^12 tiles measured 2.18 -> 2.25 ms with 16).  Every function below
+// takes a plan id.  -DOCS_PAIR_R16_MASK=(1<<e | ...) and -DOCS_PAIR_MINB_R16
+// build variant libraries with 16 values per thread at other windows.
 #ifndef OCS_PAIR_R16_MASK
 #define OCS_PAIR_R16_MASK 0
 #endif
-__host__ __device__ constexpr int pair_R(int exp)
+constexpr int kPairR16 = 32;
+__host__ __device__ constexpr int pair_e(int pid) { return pid & 31; }  // window exponent
+__host__ __device__ constexpr bool pair_r16(int pid)
 {
-    return exp <= 6 ? 16 : (((OCS_PAIR_R16_MASK) >> exp) & 1) ? 16 : 32;
+    return (pid & kPairR16) != 0 || (((OCS_PAIR_R16_MASK) >> (pid & 31)) & 1);
 }
-__host__ __device__ constexpr int pair_min_blocks(int exp);
+__host__ __device__ constexpr int pair_R(int pid) { return pair_e(pid) <= 6 || pair_r16(pid) ? 16 : 32; }
+__host__ __device__ constexpr int pair_min_blocks(int pid);
 
-__host__ __device__ constexpr FusedCfg pair_cfg(int exp)
+__host__ __device__ constexpr FusedCfg pair_cfg(int pid)
 {
-    FusedCfg c{exp, pair_R(exp), 0, {1, 1, 1, 1, 1, 1}};
+    FusedCfg c{pair_e(pid), pair_R(pid), 0, {1, 1, 1, 1, 1, 1}};
     const int lr = c.R == 32 ? 5 : 4;
-    int left = exp;  // log2 of the complex FFT size N
+    int left = pair_e(pid);  // log2 of the complex FFT size N
     int s = 0;
     while (left >= lr) { c.radix[s++] = 1 << lr; left -= lr; }
     if (left > 0) c.radix[s++] = 1 << left;
     c.nstages = s;
     return c;
 }
-__host__ __device__ constexpr int pair_T(int exp) { return (1 << exp) / pair_R(exp); }
-__host__ __device__ constexpr int pair_Ns(int exp, int s)
+__host__ __device__ constexpr int pair_T(int pid) { return (1 << pair_e(pid)) / pair_R(pid); }
+__host__ __device__ constexpr int pair_Ns(int pid, int s)
 {
     int ns = 1;
-    for (int i = 0; i < s; ++i) ns *= pair_cfg(exp).radix[i];
+    for (int i = 0; i < s; ++i) ns *= pair_cfg(pid).radix[i];
     return ns;
 }
 // twiddle table: for each stage s >= 1, (r_s - 1) * Ns(s) entries, (m-1)*Ns + j = W_{Ns r}^{j m}
-__host__ __device__ constexpr int pair_tw_offset(int exp, int s)
+__host__ __device__ constexpr int pair_tw_offset(int pid, int s)
 {
     int off = 0;
-    for (int i = 1; i < s; ++i) off += (pair_cfg(exp).radix[i] - 1) * pair_Ns(exp, i);
+    for (int i = 1; i < s; ++i) off += (pair_cfg(pid).radix[i] - 1) * pair_Ns(pid, i);
     return off;
 }
-__host__ __device__ constexpr int pair_tw_size(int exp)
+__host__ __device__ constexpr int pair_tw_size(int pid)
 {
-    return pair_tw_offset(exp, pair_cfg(exp).nstages) > 0 ? pair_tw_offset(exp, pair_cfg(exp).nstages) : 1;
+    return pair_tw_offset(pid, pair_cfg(pid).nstages) > 0 ? pair_tw_offset(pid, pair_cfg(pid).nstages) : 1;
 }
-__host__ __device__ constexpr int pair_cta_threads(int exp) { return pair_T(exp) >= 256 ? pair_T(exp) : 256; }
-__host__ __device__ constexpr int pair_ppc(int exp) { return pair_cta_threads(exp) / pair_T(exp); }  // pairs per CTA
-__host__ __device__ constexpr int pair_buf_stride(int exp) { return (1 << exp) + (1 << exp) / pair_R(exp) + 1; }
-__host__ __device__ constexpr bool pair_tables_in_smem(int exp) { return exp <= 11; }
-__host__ __device__ constexpr bool pair_supported(int exp) { return exp >= 6 && exp <= 14; }
+__host__ __device__ constexpr int pair_cta_threads(int pid) { return pair_T(pid) >= 256 ? pair_T(pid) : 256; }
+__host__ __device__ constexpr int pair_ppc(int pid) { return pair_cta_threads(pid) / pair_T(pid); }  // pairs per CTA
+__host__ __device__ constexpr int pair_buf_stride(int pid)
+{
+    return (1 << pair_e(pid)) + (1 << pair_e(pid)) / pair_R(pid) + 1;
+}
+__host__ __device__ constexpr bool pair_tables_in_smem(int pid) { return pair_e(pid) <= 11; }
+__host__ __device__ constexpr bool pair_supported(int pid) { return pair_e(pid) >= 6 && pair_e(pid) <= 14; }
 // 2 x 256 threads per SM below 2^14 (R = 16 at 2^10, three 256-thread CTAs
 // of up to 80 registers, measured 300 against 390 Gsamples/s: the extra
-// block-wide exchange costs more than the occupancy gains)
-__host__ __device__ constexpr int pair_min_blocks(int exp)
+// block-wide exchange costs more than the occupancy gains); the 16-value
+// plans of 2^12 and up have as many exchanges as the 32-value ones and run
+// three CTAs per SM
+__host__ __device__ constexpr int pair_min_blocks(int pid)
 {
 #ifdef OCS_PAIR_MINB_R16
-    if (((OCS_PAIR_R16_MASK) >> exp) & 1) return OCS_PAIR_MINB_R16;
+    if (((OCS_PAIR_R16_MASK) >> pair_e(pid)) & 1) return OCS_PAIR_MINB_R16;
 #endif
-    return pair_cta_threads(exp) >= 512 ? 1 : 512 / pair_cta_threads(exp);
+    if ((pid & kPairR16) != 0) return 3;
+    return pair_cta_threads(pid) >= 512 ? 1 : 512 / pair_cta_threads(pid);
 }
 // Twiddle entries copied to shared memory: the whole table up to 2^11; above,
 // the first exchange stage's (31 x 32 entries, 7.9 KB), which next to the
 // window still fits beside the exchange buffers at the same occupancy; the
 // later stages' twiddles are read through L1.
-__host__ __device__ constexpr int pair_smem_tw_entries(int exp)
+__host__ __device__ constexpr int pair_smem_tw_entries(int pid)
 {
-    return pair_tables_in_smem(exp) ? pair_tw_size(exp)
-                                    : (pair_cfg(exp).nstages > 2 ? pair_tw_offset(exp, 2) : pair_tw_size(exp));
+    return pair_tables_in_smem(pid) ? pair_tw_size(pid)
+                                    : (pair_cfg(pid).nstages > 2 ? pair_tw_offset(pid, 2) : pair_tw_size(pid));
 }
 // The window joins them except at 2^13, where its 32 KB would take from L1
 // what the overlapping frames' loads reuse (2^13 power: 278 Gsamples/s with
 // the window read through L1, 254 with it in shared memory).
-__host__ __device__ constexpr bool pair_smem_window(int exp) { return exp != 13; }
+__host__ __device__ constexpr bool pair_smem_window(int pid) { return pair_e(pid) != 13; }
 // From 2^12 the later stages' twiddles come from a two-level table in shared
 // memory, W_N^e = lo[e & 127] * hi[e >> 7] (128 + N/128 entries), chained
 // between sparse lookups as in the one-frame kernels, instead of the plan
 // table through L1 (at 2^14 that table is 123 KB and misses L1): 2^12 276 ->
 // 280, 2^13 268 -> 278, 2^14 211 -> 218 Gsamples/s (power).
-__host__ __device__ constexpr bool pair_tw2l(int exp) { return exp >= 12; }
-__host__ __device__ constexpr size_t pair_tw2l_bytes(int exp) { return pair_tw2l(exp) ? (128 + (1 << exp) / 128) * 8 : 0; }
-__host__ __device__ constexpr size_t pair_tab_bytes(int exp)
+__host__ __device__ constexpr bool pair_tw2l(int pid) { return pair_e(pid) >= 12; }
+__host__ __device__ constexpr size_t pair_tw2l_bytes(int pid)
 {
-    return (size_t)pair_smem_tw_entries(exp) * 8 + pair_tw2l_bytes(exp) +
-           (pair_smem_window(exp) ? (size_t)(1 << exp) * 4 : 0);
+    return pair_tw2l(pid) ? (128 + (1 << pair_e(pid)) / 128) * 8 : 0;
 }
-__host__ __device__ constexpr size_t pair_smem_bytes_ct(int exp)
+__host__ __device__ constexpr size_t pair_tab_bytes(int pid)
 {
-    return (size_t)pair_ppc(exp) * pair_buf_stride(exp) * 8 + pair_tab_bytes(exp) +
-           (size_t)(pair_cta_threads(exp) / 32) * 8 + 16;
+    return (size_t)pair_smem_tw_entries(pid) * 8 + pair_tw2l_bytes(pid) +
+           (pair_smem_window(pid) ? (size_t)(1 << pair_e(pid)) * 4 : 0);
+}
+__host__ __device__ constexpr size_t pair_smem_bytes_ct(int pid)
+{
+    return (size_t)pair_ppc(pid) * pair_buf_stride(pid) * 8 + pair_tab_bytes(pid) +
+           (size_t)(pair_cta_threads(pid) / 32) * 8 + 16;
 }
 
-template <int EXP>
+template <int EXP>  // a plan id
 struct PairCore {
     static constexpr FusedCfg C = pair_cfg(EXP);
-    static constexpr int N = 1 << EXP;
+    static constexpr int N = 1 << pair_e(EXP);
     static constexpr int R = C.R;
     static constexpr int T = N / R;
     static constexpr int NS = C.nstages;
@@ -256,7 +273,7 @@ __device__ __forceinline__ void pair_tables(const FusedArgs& a, float2* s_tab, i
                                             TwTwoLevel& tw2)
 {
     constexpr int TWN = pair_smem_tw_entries(EXP);
-    constexpr int N = 1 << EXP;
+    constexpr int N = 1 << pair_e(EXP);
     for (int i = tid; i < TWN; i += blockDim.x) s_tab[i] = a.tw[i];
     float2* s2 = s_tab + TWN;
     if constexpr (pair_tw2l(EXP)) {
@@ -310,7 +327,7 @@ stft_pair_kernel(const FusedArgs a)
         const uint64_t q = pbase + (uint64_t)gridDim.x * PPC + lp;
         if (t == 0 && q < pairs) {
             const uint64_t s0 = 2 * q * a.hop;
-            const uint64_t end = s0 + a.hop + (uint64_t)(1 << EXP);
+            const uint64_t end = s0 + a.hop + (uint64_t)(1 << pair_e(EXP));
             prefetch_l2_span(a.x, s0, end < a.n ? end : a.n);
         }
         pair_group<EXP, OUTK>(a, pbase, buf, red, s_tab, tw2, win, tid, lp, t);
@@ -340,7 +357,7 @@ __device__ __forceinline__ void pair_group(const FusedArgs& a, uint64_t pbase, f
             const uint64_t sb = sa + a.hop;
             const float* xa = a.x + sa;
             const float* xb = a.x + sb;
-            if (EXP <= 12 && act_b && sb + N <= a.n && a.hop == (uint64_t)(N / 2)) {
+            if (pair_e(EXP) <= 12 && act_b && sb + N <= a.n && a.hop == (uint64_t)(N / 2)) {
                 // frame b starts N/2 = (R/2) T samples after frame a: its slots
                 // u < R/2 are frame a's slots u + R/2, so only half of them load
                 // (1e8 samples, power: 2^9 377 -> 386, 2^10 392 -> 393, 2^12
@@ -352,7 +369,7 @@ __device__ __forceinline__ void pair_group(const FusedArgs& a, uint64_t pbase, f
                 for (int u = R / 2; u < R; ++u) v[u].y = xb[t + u * T];
 #pragma unroll
                 for (int u = 0; u < R / 2; ++u) v[u].y = v[u + R / 2].x;
-            } else if (EXP <= 12 && act_b && sb + N <= a.n && a.hop == (uint64_t)(N / 4)) {
+            } else if (pair_e(EXP) <= 12 && act_b && sb + N <= a.n && a.hop == (uint64_t)(N / 4)) {
                 // overlap 0.75: frame b's slots u < 3R/4 are frame a's slots u + R/4
 #pragma unroll
                 for (int u = 0; u < R; ++u) v[u].x = xa[t + u * T];

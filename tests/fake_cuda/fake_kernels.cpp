@@ -65,7 +65,8 @@ cudaError_t launch_pair(int exp, int outk, const FusedArgs& a, int, cudaStream_t
 }
 int pair_occupancy(int, int) { return 2; }
 int pair_per_cta(int) { return 4; }
-int pair_twiddle_count(int exp) { return 1 << exp; }
+int pair_plan_id(int exp) { return exp; }
+int pair_twiddle_count(int pid) { return 1 << (pid & 31); }
 cudaError_t build_pair_twiddles(float2*, int, cudaStream_t) { return no_work(); }
 
 bool batch_supports(int exp) { return exp >= 6 && exp <= 13; }
