@@ -344,7 +344,7 @@ int prepare(uint64_t n, int exp, float ov, const char* options, Request& r)
     if (r.opt.precision >= 1 && !ocs::tc_supports(exp))
         return fail(OCS_EINVAL, "the tensor-core form supports windows 2^8 .. 2^12");
     if (r.opt.precision >= 1 && !ocs::tc_mode_supported(exp, r.opt.precision))
-        return fail(OCS_EINVAL, "the bf16 hi/mid/lo tensor-core form does not fit window 2^12");
+        return fail(OCS_EINVAL, "this tensor-core split mode is not available at this window size");
     if (r.opt.precision >= 2 && !ocs::tc_piped(exp, r.geo.hop))
         return fail(OCS_EINVAL, "the bf16 tensor-core forms need a frame advance of at most the window");
     r.exp = exp;

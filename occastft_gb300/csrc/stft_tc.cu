@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(128, 1) stft_tc_kernel(const FusedArgs a, int*
     const uint32_t a1 = smem_u32(A1), a2 = smem_u32(A2), b1 = smem_u32(B1), b2 = smem_u32(B2);
 
     const uint64_t ntiles = (a.frames + FPT - 1) / FPT;
-    uint32_t phase = 0;
+    uint32_t phase = 0, phase1 = 0;  // parities of the pass-1 and pass-2 barriers
     bool aborted = false;
     for (uint64_t tile = blockIdx.x; tile < ntiles && !aborted; tile += gridDim.x) {
         const uint64_t f0 = tile * FPT;
@@ -1087,16 +1087,24 @@ struct TcgCfg {
     static constexpr int K2 = 2 * Q, NO2 = 2 * Q;  // pass 2
     static constexpr int KP2 = (K2 + 63) / 64;  // B2 panels of 64 K
     static constexpr uint32_t A1_PART = (K1 / 8) * 2048;  // 128 rows, MN-major
-    static constexpr uint32_t A2_PART = (K2 / 8) * 2048;
+    static constexpr uint32_t A2_PART_FULL = (K2 / 8) * 2048;
     static constexpr uint32_t A1_BYTES = PARTS * A1_PART;
-    static constexpr uint32_t A2_BLOCK = PARTS * A2_PART;
-    static constexpr uint32_t A2_BYTES = MB * A2_BLOCK;
-    static constexpr uint32_t A_BYTES = A1_BYTES > A2_BYTES ? A1_BYTES : A2_BYTES;
     static constexpr uint32_t B1_PART = NO1 * 128;  // K1 <= 64: one 128-byte row per output column
     static constexpr uint32_t B2_PANEL = NO2 * 128;
     static constexpr uint32_t B2_PART = KP2 * B2_PANEL;
     static constexpr uint32_t B1_BYTES = PARTS * B1_PART;
     static constexpr uint32_t B2_BYTES = PARTS * B2_PART;
+    // Pass 2 in two halves of K (real parts, then imaginary parts, through one
+    // A2 buffer of half the size) where the whole A2 does not fit beside the
+    // DFT matrices: 4096 = 64 x 64 with bf16 hi/mid/lo operands (242 KB whole)
+    static constexpr uint32_t A2_WHOLE_BYTES = MB * PARTS * A2_PART_FULL;
+    static constexpr uint32_t SMEM_WHOLE = (A1_BYTES > A2_WHOLE_BYTES ? A1_BYTES : A2_WHOLE_BYTES) + B1_BYTES +
+                                           B2_BYTES + 128 * 8 + 256 + 1024;
+    static constexpr int KH = (SMEM_WHOLE > 227 * 1024 && MB == 1 && Q % 16 == 0) ? 2 : 1;
+    static constexpr uint32_t A2_PART = A2_PART_FULL / KH;  // one K half (or the whole K)
+    static constexpr uint32_t A2_BLOCK = PARTS * A2_PART;
+    static constexpr uint32_t A2_BYTES = MB * A2_BLOCK;
+    static constexpr uint32_t A_BYTES = A1_BYTES > A2_BYTES ? A1_BYTES : A2_BYTES;
     static constexpr uint32_t OFF_A = 0;
     static constexpr uint32_t OFF_B1 = OFF_A + A_BYTES;
     static constexpr uint32_t OFF_B2 = OFF_B1 + B1_BYTES;
@@ -1188,7 +1196,7 @@ __global__ void __launch_bounds__(128, 1) stft_tcg_kernel(const FusedArgs a, int
     const uint32_t sa = smem_u32(A), sb1 = smem_u32(B1), sb2 = smem_u32(B2);
 
     const uint64_t ntiles = (a.frames + FPT - 1) / FPT;
-    uint32_t phase = 0;
+    uint32_t phase = 0, phase1 = 0;  // parities of the pass-1 and pass-2 barriers
     bool aborted = false;
     for (uint64_t tile = blockIdx.x; tile < ntiles && !aborted; tile += gridDim.x) {
         const uint64_t f0 = tile * FPT;
@@ -1292,67 +1300,88 @@ __global__ void __launch_bounds__(128, 1) stft_tcg_kernel(const FusedArgs a, int
             break;
         }
         fence_after();
-        // ---------------- epilogue 1: twiddle, scale by 1/P, split -> A2 (row = this thread)
-        {
-            const int lf = tid / Q, g = tid % Q;
-            constexpr float inv_p = 1.0f / (float)P;
+        // ---------------- epilogue 1 and pass 2, over the K halves of pass 2 (one
+        // half, the whole K, unless the whole A2 does not fit)
 #pragma unroll 1
-            for (int k1b = 0; k1b < P; k1b += 8) {
-                float t[16];
-                tmem_ld16(d1 + lane_base + 2 * k1b, t);
-                float re[8], im[8];
-#pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    const int e = (g * (k1b + q)) & (N - 1);
-                    const float2 w = cmul2(TWL[e & 63], TWL[64 + (e >> 6)]);
-                    const float yr = t[2 * q], yi = t[2 * q + 1];
-                    re[q] = (yr * w.x - yi * w.y) * inv_p;
-                    im[q] = (yr * w.y + yi * w.x) * inv_p;
-                }
-                uint4 pr_[PARTS], pi_[PARTS];
-                S::split8(re, pr_);
-                S::split8(im, pi_);
-                const int row2 = lf * P + k1b;  // 8 consecutive pass-2 rows, one block
-                unsigned char* blk = A + (row2 >> 7) * C::A2_BLOCK;
-                const uint32_t or_ = mn_off(row2 & 127, g), oi_ = mn_off(row2 & 127, Q + g);
-#pragma unroll
-                for (int k = 0; k < PARTS; ++k) {
-                    *reinterpret_cast<uint4*>(blk + k * C::A2_PART + or_) = pr_[k];
-                    *reinterpret_cast<uint4*>(blk + k * C::A2_PART + oi_) = pi_[k];
-                }
+        for (int h = 0; h < C::KH; ++h) {
+            if (h > 0) {
+                // the previous half's MMAs have read A2 (their commit arrived)
+                fence_before();
+                __syncthreads();
+                fence_after();
             }
-        }
-        fence_async_smem();
-        fence_before();
-        __syncthreads();
-        fence_after();
-        // ---------------- pass 2 on the tensor cores, one MMA chain per 128-row block
-        if (tid == 0) {
+            // epilogue 1: twiddle, scale by 1/P, split -> A2 (row = this thread)
+            {
+                const int lf = tid / Q, g = tid % Q;
+                constexpr float inv_p = 1.0f / (float)P;
+#pragma unroll 1
+                for (int k1b = 0; k1b < P; k1b += 8) {
+                    float t[16];
+                    tmem_ld16(d1 + lane_base + 2 * k1b, t);
+                    float re[8], im[8];
 #pragma unroll
-            for (int b = 0; b < MB; ++b) {
+                    for (int q = 0; q < 8; ++q) {
+                        const int e = (g * (k1b + q)) & (N - 1);
+                        const float2 w = cmul2(TWL[e & 63], TWL[64 + (e >> 6)]);
+                        const float yr = t[2 * q], yi = t[2 * q + 1];
+                        re[q] = (yr * w.x - yi * w.y) * inv_p;
+                        im[q] = (yr * w.y + yi * w.x) * inv_p;
+                    }
+                    const int row2 = lf * P + k1b;  // 8 consecutive pass-2 rows, one block
+                    unsigned char* blk = A + (row2 >> 7) * C::A2_BLOCK;
+                    if (C::KH == 1 || h == 0) {
+                        uint4 pr_[PARTS];
+                        S::split8(re, pr_);
+                        const uint32_t or_ = mn_off(row2 & 127, g);
 #pragma unroll
-                for (int ks = 0; ks < C::K2 / 16; ++ks) {
+                        for (int k = 0; k < PARTS; ++k) *reinterpret_cast<uint4*>(blk + k * C::A2_PART + or_) = pr_[k];
+                    }
+                    if (C::KH == 1 || h == 1) {
+                        uint4 pi_[PARTS];
+                        S::split8(im, pi_);
+                        const uint32_t oi_ = mn_off(row2 & 127, (C::KH == 1 ? Q : 0) + g);
 #pragma unroll
-                    for (int pr = 0; pr < NPROD; ++pr) {
-                        const uint64_t ad =
-                            sdesc(sa + b * C::A2_BLOCK + PA[pr] * C::A2_PART + ks * 4096, 1024, 2048);
-                        const uint64_t bd =
-                            sdesc(sb2 + PB[pr] * C::B2_PART + (ks >> 2) * C::B2_PANEL + (ks & 3) * 32, 16, 1024);
-                        mma_f16(d2 + b * C::NO2, ad, bd, ID2, (ks > 0 || pr > 0) ? 1u : 0u);
+                        for (int k = 0; k < PARTS; ++k) *reinterpret_cast<uint4*>(blk + k * C::A2_PART + oi_) = pi_[k];
                     }
                 }
             }
-            mma_commit(&mbar[1]);
+            fence_async_smem();
+            fence_before();
+            __syncthreads();
+            fence_after();
+            // pass 2 on the tensor cores, one MMA chain per 128-row block: K slices
+            // [h KS, h KS + KS) of the complex Q-point DFT, this half's A2 at slice 0
+            constexpr int KS = C::K2 / 16 / C::KH;
+            if (tid == 0) {
+#pragma unroll
+                for (int b = 0; b < MB; ++b) {
+#pragma unroll
+                    for (int kk = 0; kk < KS; ++kk) {
+                        const int ks = h * KS + kk;
+#pragma unroll
+                        for (int pr = 0; pr < NPROD; ++pr) {
+                            const uint64_t ad =
+                                sdesc(sa + b * C::A2_BLOCK + PA[pr] * C::A2_PART + kk * 4096, 1024, 2048);
+                            const uint64_t bd =
+                                sdesc(sb2 + PB[pr] * C::B2_PART + (ks >> 2) * C::B2_PANEL + (ks & 3) * 32, 16, 1024);
+                            mma_f16(d2 + b * C::NO2, ad, bd, ID2, (ks > 0 || pr > 0) ? 1u : 0u);
+                        }
+                    }
+                }
+                mma_commit(&mbar[1]);
+            }
+            if (!mbar_wait(&mbar[1], phase1)) {
+                if (lane == 0) atomicExch(abort_flag, 1);
+            }
+            phase1 ^= 1u;
+            __syncthreads();
+            if (*abort_flag) break;
+            fence_after();
         }
-        if (!mbar_wait(&mbar[1], phase)) {
-            if (lane == 0) atomicExch(abort_flag, 1);
-        }
-        __syncthreads();
         if (*abort_flag) {
             aborted = true;
             break;
         }
-        fence_after();
         // ---------------- epilogue 2: thread = (frame, k1) of each block holds X[k1 + P k2]
 #pragma unroll 1
         for (int b = 0; b < MB; ++b) {
@@ -1545,9 +1574,8 @@ bool tc_supports(int exp) { return exp >= 8 && exp <= 12; }
 
 bool tc_mode_supported(int exp, int pm)
 {
-    if (!tc_supports(exp)) return false;
-    // the generic form's bf16 hi/mid/lo operands at 4096 exceed shared memory
-    return !(exp == 12 && pm == PM_BF16X3);
+    (void)pm;  // every split mode at every size (bf16 hi/mid/lo at 4096 takes pass 2 in K halves)
+    return tc_supports(exp);
 }
 
 // whether every split mode is available for this frame advance: the

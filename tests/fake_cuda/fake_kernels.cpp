@@ -128,7 +128,7 @@ int pairx2_occupancy(int, int) { return 2; }
 int pairx2_per_cta(int) { return 8; }
 
 bool tc_supports(int exp) { return exp >= 8 && exp <= 12; }
-bool tc_mode_supported(int exp, int pm) { return !(exp == 12 && pm == 3); }
+bool tc_mode_supported(int exp, int) { return exp >= 8 && exp <= 12; }
 bool tc_piped(int exp, uint64_t hop) { return (exp != 8 && exp != 10) || hop <= (1ull << exp); }
 cudaError_t launch_tc(int exp, int outk, int, const FusedArgs& a, int*, int, int, cudaStream_t st)
 {

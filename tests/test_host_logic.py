@@ -211,8 +211,6 @@ def test_validation_before_any_device_call(ocs_lib):
     err(L.ocs_activate_device(P, 100000, 10, 0.5, b"", None, g.out_floats, None), ocs_lib.OCS_EINVAL, "null")
     err(L.ocs_activate(P, 100000, 7, 0.5, b"--precision=tc-fp16", P, 1 << 30, ctypes.byref(n_out)),
         ocs_lib.OCS_EINVAL, "2^8 .. 2^12")
-    err(L.ocs_activate(P, 100000, 12, 0.5, b"--precision=tc-bf16x3", P, 1 << 30, ctypes.byref(n_out)),
-        ocs_lib.OCS_EINVAL, "does not fit")
     # a negative overlap ratio (accepted, as in the reference) advances frames by more than N
     assert ocs_lib.geometry(100000, 8, -0.5, "").hop == 384
     err(L.ocs_activate(P, 100000, 8, -0.5, b"--precision=tc-bf16x2", P, 1 << 30, ctypes.byref(n_out)),
