@@ -14,6 +14,7 @@
 // Window_* -> DCRemove_Common -> FFT -> toPower (OKL/EXPCommon.okl:7-245,
 // OKL/kernel.okl:178-194).
 #pragma once
+#include "ocs_x2.cuh"
 #include "stft_fused_kernel.cuh"
 
 #include <type_traits>
@@ -192,18 +193,25 @@ __device__ __forceinline__ void tpfl_group(const FusedArgs& a, uint64_t g, float
             y0[p] = make_float2(d.x * w.x, d.y * w.y);
             y1[p] = make_float2(d.z * w.z, d.w * w.w);
         }
+        // the combinations on packed FP32x2 (both components of a complex
+        // value in one instruction; each component's rounding is unchanged).
+        // The window products stay scalar: from the parameter bank they take
+        // the coefficient as an operand, and packed ones made the batch
+        // kernel spill.
         if constexpr (L == 2) {
             // z0 + (-1)^q z1
-            v[2 * c] = make_float2(fmaf(cr, y0[1].x, y0[0].x), fmaf(cr, y0[1].y, y0[0].y));
-            v[2 * c + 1] = make_float2(fmaf(cr, y1[1].x, y1[0].x), fmaf(cr, y1[1].y, y1[0].y));
+            v[2 * c] = x2::fma2(x2::bc(cr), y0[1], y0[0]);
+            v[2 * c + 1] = x2::fma2(x2::bc(cr), y1[1], y1[0]);
         } else {
             // (z0 + (-1)^q z2) + W_4^q (z1 + (-1)^q z3)
             static_for<0, 2>([&](auto hc) {
                 constexpr int h = decltype(hc)::value;
                 const float2* y = h ? y1 : y0;
-                const float2 P = make_float2(fmaf(s2, y[2].x, y[0].x), fmaf(s2, y[2].y, y[0].y));
-                const float2 Q = make_float2(fmaf(s2, y[3].x, y[1].x), fmaf(s2, y[3].y, y[1].y));
-                v[2 * c + h] = make_float2(fmaf(cr, Q.x, fmaf(-ci, Q.y, P.x)), fmaf(cr, Q.y, fmaf(ci, Q.x, P.y)));
+                const float2 P = x2::fma2(x2::bc(s2), y[2], y[0]);
+                const float2 Q = x2::fma2(x2::bc(s2), y[3], y[1]);
+                // (cr Q.x + (-ci Q.y + P.x), cr Q.y + (ci Q.x + P.y))
+                const float2 inner = x2::fma2(make_float2(-ci, ci), make_float2(Q.y, Q.x), P);
+                v[2 * c + h] = x2::fma2(x2::bc(cr), Q, inner);
             });
         }
     }
