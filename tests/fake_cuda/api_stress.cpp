@@ -326,6 +326,43 @@ void batch()
     std::printf("ok %s\n", name);
 }
 
+void batch_tune()
+{
+    const char* name = "batch_tune";
+    setenv("OCS_AUTOTUNE", "1", 1);
+    cudaStream_t st;
+    check(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess, name, "stream");
+    std::vector<DevReq> v = make_batch(31, 60);
+    std::vector<ocs_request> q = requests(v);
+    // a new mix: every tile length is timed (4 lengths x 3 launches), then the batch runs once more
+    long l0 = fake::launches.load();
+    check(ocs_batch_device(q.data(), (int)q.size(), st) == OCS_OK, name, "tuned launch");
+    cudaStreamSynchronize(st);
+    check(fake::launches.load() - l0 == 13, name, "launches " + std::to_string(fake::launches.load() - l0));
+    check_batch(v, q, name);
+    // the same mix again: the kept choice, one launch
+    l0 = fake::launches.load();
+    check(ocs_batch_device(q.data(), (int)q.size(), st) == OCS_OK, name, "second launch");
+    cudaStreamSynchronize(st);
+    check(fake::launches.load() - l0 == 1, name, "second call tuned again");
+    check_batch(v, q, name);
+    // a fixed length: no timing for a new mix either
+    free_batch(v);
+    v = make_batch(32, 20);
+    q = requests(v);
+    setenv("OCS_BATCH_GROUPS", "32", 1);
+    l0 = fake::launches.load();
+    check(ocs_batch_device(q.data(), (int)q.size(), st) == OCS_OK, name, "fixed length");
+    cudaStreamSynchronize(st);
+    check(fake::launches.load() - l0 == 1, name, "fixed length timed");
+    check_batch(v, q, name);
+    unsetenv("OCS_BATCH_GROUPS");
+    free_batch(v);
+    cudaStreamDestroy(st);
+    setenv("OCS_AUTOTUNE", "0", 1);
+    std::printf("ok %s\n", name);
+}
+
 void capture()
 {
     const char* name = "capture";
@@ -502,6 +539,7 @@ int main(int argc, char** argv)
     activate();
     concurrent();
     batch();
+    batch_tune();
     capture();
     shutdown();
     std::printf("all ok\n");

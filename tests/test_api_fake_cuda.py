@@ -12,8 +12,9 @@ Covers what the GPU tests cannot make happen on purpose or often enough:
   signal in three placements;
 - four threads calling ocs_activate at once;
 - ocs_plan_tune ahead of a request (its scratch released, the choice kept);
-- uneven batches, the per-capture descriptor buffers, and a full release at
-  ocs_shutdown."""
+- uneven batches, the tile-length tuning of a new mix (timed once, then kept;
+  none with a fixed length), the per-capture descriptor buffers, and a full
+  release at ocs_shutdown."""
 import os
 import shutil
 import subprocess
@@ -27,7 +28,7 @@ SOURCES = [os.path.join(CSRC, "ocs_api.cpp"), os.path.join(CSRC, "ocs_host.cpp")
            os.path.join(FAKE, "fake_runtime.cpp"), os.path.join(FAKE, "fake_kernels.cpp"),
            os.path.join(FAKE, "api_stress.cpp")]
 CHECKS = ["setup_fail", "table_fail", "slot_fail", "tune_fail", "capture_tune", "plan_tune", "activate",
-          "concurrent", "batch", "capture", "shutdown"]
+          "concurrent", "batch", "batch_tune", "capture", "shutdown"]
 
 
 def _build(out, sanitize):
